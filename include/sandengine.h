@@ -1,0 +1,141 @@
+/*
+ * sandengine_gb300 C ABI: the Margolus 2x2 block grid update of sandengine on GB300.
+ *
+ * This is the drop-in boundary for the reference's simulation path.  A host binds these
+ * functions (Rust extern "C", ctypes, ...) in place of:
+ *   - sandengine-lang: parse_string / parse_path / create_glsl_from_parser
+ *       (sandengine-lang/src/parser.rs:93-152, sandengine-lang/src/lib.rs:10-17)
+ *   - sandengine-core::simulation::Simulation: new / run / params.frame / modifications
+ *       (sandengine-core/src/simulation.rs:97-253)
+ *
+ * Conventions: every function returns an int status (SE_OK = 0); on failure
+ * se_last_error() returns a message for the calling thread.  Nothing aborts or throws
+ * across the boundary.  Handles are not thread-safe; distinct handles may be used from
+ * distinct threads.  Cells are uint32 material ids (the reference stores the id in the .r
+ * channel of an RGBA32F texel, operations.glsl:111-112); ids that name no material read
+ * as NULL, as getMaterialFromID does (gen/materials.glsl:79-86).
+ */
+#ifndef SANDENGINE_GB300_H
+#define SANDENGINE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The parse kinds mirror ParsingErr (sandengine-lang/src/parser.rs:42-73). */
+enum se_status {
+  SE_OK = 0,
+  SE_ERR_INVALID_ARGUMENT = 1,
+  SE_ERR_MISSING_FIELD = 2,   /* ParsingErr::MissingField */
+  SE_ERR_INVALID_TYPE = 3,    /* ParsingErr::InvalidType */
+  SE_ERR_NOT_FOUND = 4,       /* ParsingErr::NotFound */
+  SE_ERR_NOT_RECOGNIZED = 5,  /* ParsingErr::NotRecognized */
+  SE_ERR_YAML = 6,            /* serde_yaml rejected the text */
+  SE_ERR_PANIC = 7,           /* the reference panics on this input (e.g. unknown parent type) */
+  SE_ERR_GLSL = 8,            /* the generated shader would not compile (reference panics, simulation.rs:133-137) */
+  SE_ERR_UNSUPPORTED = 9,     /* valid rule GLSL the CUDA back end does not translate */
+  SE_ERR_COMPILE = 10,        /* NVRTC failed */
+  SE_ERR_CUDA = 11,           /* a CUDA runtime call failed */
+  SE_ERR_OUT_OF_MEMORY = 12,
+  SE_ERR_BUFFER_TOO_SMALL = 13,
+  SE_ERR_NOT_COMPILED = 14,   /* se_ruleset_compile has not succeeded yet */
+  SE_ERR_BUDGET = 15,         /* serving: the request cannot fit the HBM budget */
+  SE_ERR_TIMEOUT = 16
+};
+
+/* Modification shapes (sandengine-core/src/simulation.rs:41-42). */
+#define SE_MODSHAPE_CIRCLE 0
+#define SE_MODSHAPE_SQUARE 1
+#define SE_MAX_MODIFICATIONS 256 /* simulation.rs:43 */
+
+/* SimModification, repr(C), 32 bytes = the std140 UBO record (simulation.rs:45-56). */
+typedef struct se_modification {
+  int32_t position[2];
+  int32_t mod_shape;
+  int32_t mod_size;
+  int32_t mod_matID;
+  int32_t _pad4[3];
+} se_modification;
+
+typedef struct se_ruleset se_ruleset;
+typedef struct se_world se_world;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* se_last_error(void);
+/* Library version as 10000*major + 100*minor + patch. */
+int se_version(void);
+
+/* ---- rule language (replaces sandengine-lang; no GPU needed) ------------------------- */
+
+/* parse_string (parser.rs:93-152): parses the YAML rule set and generates the CUDA rule
+ * code.  Parse errors return SE_ERR_MISSING_FIELD / _INVALID_TYPE / _NOT_FOUND /
+ * _NOT_RECOGNIZED / _YAML / _PANIC with the reference's message text in se_last_error().
+ * Rule text whose GLSL would not compile (SE_ERR_GLSL) or that the CUDA back end does not
+ * translate (SE_ERR_UNSUPPORTED) parses, and fails in se_ruleset_compile / se_world_create,
+ * where the reference panics building its shader (simulation.rs:133-137). */
+int se_ruleset_parse(const char* yaml_text, se_ruleset** out);
+/* parse_path (sandengine-lang/src/lib.rs:10-13). */
+int se_ruleset_parse_path(const char* path, se_ruleset** out);
+/* create_glsl_from_parser (sandengine-lang/src/lib.rs:17-147), returned as text:
+ * which = 0 -> gen/materials.glsl, 1 -> gen/rules.glsl, 2 -> generated CUDA rule code,
+ * 3 -> the complete device source handed to NVRTC.
+ * Writes at most cap bytes (NUL-terminated when room); *len gets the full length. */
+int se_ruleset_text(const se_ruleset* rs, int which, char* buf, size_t cap, size_t* len);
+/* Compiles the rule set's kernels for sm_103a with NVRTC (cached on disk under
+ * $SE_CACHE_DIR or ~/.cache/sandengine_gb300).  Needs no GPU. */
+int se_ruleset_compile(se_ruleset* rs);
+/* Number of materials (ids 0..n-1; EMPTY=0, NULL=1, WALL=2, then YAML order). */
+int se_ruleset_num_materials(const se_ruleset* rs, int* n);
+/* Material id by name (materials.rs ids), or SE_ERR_NOT_FOUND. */
+int se_ruleset_material_id(const se_ruleset* rs, const char* name, int* id);
+void se_ruleset_free(se_ruleset* rs);
+
+/* ---- one world (replaces sandengine-core::simulation::Simulation) --------------------- */
+
+/* Simulation::new (simulation.rs:128-192): an all-EMPTY width x height world with frame
+ * counter 0 on the current CUDA device.  Compiles the rule set if needed. */
+int se_world_create(se_ruleset* rs, int width, int height, se_world** out);
+void se_world_destroy(se_world* w);
+/* Work is issued on this stream (cudaStream_t; NULL = the world's own stream). */
+int se_world_set_stream(se_world* w, void* cuda_stream);
+int se_world_get_stream(se_world* w, void** cuda_stream);
+/* Fusion depth: frames advanced per launch when no edit intervenes (1 = one launch per
+ * frame, like the reference; 0 = the library's tuned default). */
+int se_world_set_steps_per_launch(se_world* w, int k);
+/* Replace / read the grid (width*height uint32, row-major) from host memory.  Both
+ * synchronize the world's stream. */
+int se_world_set_grid(se_world* w, const uint32_t* cells, size_t count);
+int se_world_get_grid(se_world* w, uint32_t* cells, size_t count);
+/* Stream-ordered copies with pinned host memory that the caller keeps alive until the
+ * stream reaches them. */
+int se_world_set_grid_async(se_world* w, const uint32_t* cells, size_t count);
+int se_world_get_grid_async(se_world* w, uint32_t* cells, size_t count);
+/* Device pointer of the current grid (valid until the next step, which ping-pongs). */
+int se_world_device_grid(se_world* w, uint32_t** device_cells);
+/* Params.frame (simulation.rs:78): the counter before the next step (>= 0). */
+int se_world_set_frame(se_world* w, int32_t frame);
+int se_world_get_frame(const se_world* w, int32_t* frame);
+/* Simulation::run repeated nframes times (simulation.rs:195-253): each frame does
+ * frame += 1 and one Margolus step (frame 1 clears the grid, falling_sand.glsl:128-131).
+ * `mods` (up to 256 used, the scan stops at the first mod_size == 0) apply to the first
+ * of these frames only, as the reference clears its list after each run.  Asynchronous on
+ * the world's stream. */
+int se_world_step(se_world* w, int nframes, const se_modification* mods, int nmods);
+int se_world_synchronize(se_world* w);
+/* Order-independent 64-bit digest of the current grid: sum over cells i of
+ * splitmix64_finalize((i << 32) | cell[i]) mod 2^64.  Synchronizes the stream.
+ * (No counterpart in the reference: a device-side check for full-size worlds.) */
+int se_world_digest(se_world* w, uint64_t* digest);
+/* counts[m] = number of cells holding value m, for m < nbins-1; counts[nbins-1] gets all
+ * values >= nbins-1.  nbins in [1, 257].  Synchronizes the stream.  (No counterpart in the
+ * reference: material-conservation checks.) */
+int se_world_histogram(se_world* w, uint64_t* counts, int nbins);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SANDENGINE_GB300_H */

@@ -1,0 +1,278 @@
+// The C ABI (include/sandengine.h).  Every entry point catches everything: no exception
+// or abort crosses the boundary.
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+#include <string>
+
+#include "../../include/sandengine.h"
+#include "lang/codegen.hpp"
+#include "lang/lang.hpp"
+#include "runtime/engine.hpp"
+
+#define SE_API extern "C" __attribute__((visibility("default")))
+
+struct se_ruleset {
+  std::shared_ptr<se::rt::Ruleset> rs;
+};
+struct se_world {
+  std::unique_ptr<se::rt::World> w;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+int ret(const se::rt::Status& s) {
+  if (!s.ok()) return fail(s.code, s.msg);
+  return SE_OK;
+}
+
+int parse_kind_code(const std::string& kind) {
+  if (kind == "MissingField") return SE_ERR_MISSING_FIELD;
+  if (kind == "InvalidType") return SE_ERR_INVALID_TYPE;
+  if (kind == "NotFound") return SE_ERR_NOT_FOUND;
+  if (kind == "NotRecognized") return SE_ERR_NOT_RECOGNIZED;
+  if (kind == "Yaml") return SE_ERR_YAML;
+  if (kind == "Panic") return SE_ERR_PANIC;
+  if (kind == "Glsl") return SE_ERR_GLSL;
+  if (kind == "Unsupported") return SE_ERR_UNSUPPORTED;
+  return SE_ERR_INVALID_ARGUMENT;
+}
+
+template <class F>
+int guard(F&& f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    return fail(SE_ERR_OUT_OF_MEMORY, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(SE_ERR_INVALID_ARGUMENT, e.what());
+  } catch (...) {
+    return fail(SE_ERR_INVALID_ARGUMENT, "unknown error");
+  }
+}
+
+}  // namespace
+
+SE_API const char* se_last_error(void) { return g_last_error.c_str(); }
+SE_API int se_version(void) { return 100; }
+
+SE_API int se_ruleset_parse(const char* yaml_text, se_ruleset** out) {
+  return guard([&] {
+    if (!yaml_text || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    auto rs = std::make_shared<se::rt::Ruleset>();
+    se::lang::ParseError err;
+    if (!se::lang::parse_string(yaml_text, &rs->parsed, &err)) return fail(parse_kind_code(err.kind), err.message);
+    rs->materials_glsl = se::lang::materials_glsl(rs->parsed);
+    rs->rules_glsl = se::lang::rules_glsl(rs->parsed);
+    // Like the reference, parsing succeeds even when the generated rule code cannot be
+    // built; that failure is reported when the kernels are built (se_ruleset_compile,
+    // se_world_create), where the reference panics building its shader.
+    if (!se::lang::generate_cuda(rs->parsed, &rs->cuda, &err)) {
+      rs->codegen_code = parse_kind_code(err.kind);
+      rs->codegen_message = err.message;
+    }
+    *out = new se_ruleset{rs};
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_ruleset_parse_path(const char* path, se_ruleset** out) {
+  return guard([&] {
+    if (!path || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(SE_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    std::string text = ss.str();
+    return se_ruleset_parse(text.c_str(), out);
+  });
+}
+
+SE_API int se_ruleset_text(const se_ruleset* rs, int which, char* buf, size_t cap, size_t* len) {
+  return guard([&] {
+    if (!rs) return fail(SE_ERR_INVALID_ARGUMENT, "null ruleset");
+    const std::string* s;
+    std::string full;
+    if (which == 0) s = &rs->rs->materials_glsl;
+    else if (which == 1) s = &rs->rs->rules_glsl;
+    else if (which == 2) s = &rs->rs->cuda.source;
+    else if (which == 3) s = &(full = se::rt::kernel_source(rs->rs->cuda.source));
+    else return fail(SE_ERR_INVALID_ARGUMENT, "which must be 0, 1, 2 or 3");
+    if (len) *len = s->size();
+    if (buf && cap) {
+      size_t n = std::min(cap - 1, s->size());
+      memcpy(buf, s->data(), n);
+      buf[n] = '\0';
+      if (n < s->size()) return fail(SE_ERR_BUFFER_TOO_SMALL, "buffer too small");
+    }
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_ruleset_compile(se_ruleset* rs) {
+  return guard([&] {
+    if (!rs) return fail(SE_ERR_INVALID_ARGUMENT, "null ruleset");
+    return ret(rs->rs->compile());
+  });
+}
+
+SE_API int se_ruleset_num_materials(const se_ruleset* rs, int* n) {
+  return guard([&] {
+    if (!rs || !n) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *n = rs->rs->num_materials();
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_ruleset_material_id(const se_ruleset* rs, const char* name, int* id) {
+  return guard([&] {
+    if (!rs || !name || !id) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    for (auto& m : rs->rs->parsed.materials)
+      if (m.name == name) {
+        *id = (int)m.id;
+        return (int)SE_OK;
+      }
+    return fail(SE_ERR_NOT_FOUND, std::string("no material named ") + name);
+  });
+}
+
+SE_API void se_ruleset_free(se_ruleset* rs) { delete rs; }
+
+SE_API int se_world_create(se_ruleset* rs, int width, int height, se_world** out) {
+  return guard([&] {
+    if (!rs || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    auto w = std::make_unique<se::rt::World>();
+    se::rt::Status s = w->create(rs->rs, width, height);
+    if (!s.ok()) return ret(s);
+    *out = new se_world{std::move(w)};
+    return (int)SE_OK;
+  });
+}
+
+SE_API void se_world_destroy(se_world* w) {
+  if (w && w->w && w->w->stream) cudaStreamSynchronize(w->w->stream);
+  delete w;
+}
+
+SE_API int se_world_set_stream(se_world* w, void* s) {
+  return guard([&] {
+    if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
+    w->w->stream = s ? (cudaStream_t)s : w->w->own_stream;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_get_stream(se_world* w, void** s) {
+  return guard([&] {
+    if (!w || !s) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *s = (void*)w->w->stream;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_set_steps_per_launch(se_world* w, int k) {
+  return guard([&] {
+    if (!w || k < 0) return fail(SE_ERR_INVALID_ARGUMENT, "bad argument");
+    int kmax = 0;
+    for (auto& t : se::rt::tile_variants()) kmax = std::max(kmax, t.kmax);
+    if (k > kmax) return fail(SE_ERR_INVALID_ARGUMENT, "at most " + std::to_string(kmax) + " frames per launch");
+    w->w->steps_per_launch = k;
+    return (int)SE_OK;
+  });
+}
+
+namespace {
+int grid_copy(se_world* w, void* host, size_t count, bool to_device, bool sync) {
+  if (!w || !host) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+  auto& W = *w->w;
+  if (count != (size_t)W.W * W.H) return fail(SE_ERR_INVALID_ARGUMENT, "count must be width*height");
+  const size_t bytes = count * sizeof(uint32_t);
+  cudaError_t e = to_device ? cudaMemcpyAsync(W.buf[W.cur], host, bytes, cudaMemcpyHostToDevice, W.stream)
+                            : cudaMemcpyAsync(host, W.buf[W.cur], bytes, cudaMemcpyDeviceToHost, W.stream);
+  if (e == cudaSuccess && sync) e = cudaStreamSynchronize(W.stream);
+  if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("grid copy: ") + cudaGetErrorString(e));
+  return (int)SE_OK;
+}
+}  // namespace
+
+SE_API int se_world_set_grid(se_world* w, const uint32_t* cells, size_t count) {
+  return guard([&] { return grid_copy(w, (void*)cells, count, true, true); });
+}
+SE_API int se_world_get_grid(se_world* w, uint32_t* cells, size_t count) {
+  return guard([&] { return grid_copy(w, cells, count, false, true); });
+}
+SE_API int se_world_set_grid_async(se_world* w, const uint32_t* cells, size_t count) {
+  return guard([&] { return grid_copy(w, (void*)cells, count, true, false); });
+}
+SE_API int se_world_get_grid_async(se_world* w, uint32_t* cells, size_t count) {
+  return guard([&] { return grid_copy(w, cells, count, false, false); });
+}
+
+SE_API int se_world_device_grid(se_world* w, uint32_t** p) {
+  return guard([&] {
+    if (!w || !p) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *p = w->w->buf[w->w->cur];
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_set_frame(se_world* w, int32_t frame) {
+  return guard([&] {
+    if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
+    if (frame < 0) return fail(SE_ERR_INVALID_ARGUMENT, "frame must be >= 0 (frame % 4 of a negative is undefined in GLSL)");
+    w->w->frame = frame;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_get_frame(const se_world* w, int32_t* frame) {
+  return guard([&] {
+    if (!w || !frame) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *frame = w->w->frame;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_step(se_world* w, int nframes, const se_modification* mods, int nmods) {
+  return guard([&] {
+    if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
+    return ret(w->w->step(nframes, mods, nmods));
+  });
+}
+
+SE_API int se_world_synchronize(se_world* w) {
+  return guard([&] {
+    if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
+    cudaError_t e = cudaStreamSynchronize(w->w->stream);
+    if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_digest(se_world* w, uint64_t* digest) {
+  return guard([&] {
+    if (!w || !digest) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    unsigned long long d = 0;
+    se::rt::Status s = w->w->digest(&d);
+    if (!s.ok()) return ret(s);
+    *digest = d;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_histogram(se_world* w, uint64_t* counts, int nbins) {
+  return guard([&] {
+    if (!w || !counts) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(w->w->histogram(reinterpret_cast<unsigned long long*>(counts), nbins));
+  });
+}

@@ -1,0 +1,173 @@
+#include "jit.hpp"
+
+#include <nvrtc.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <functional>
+#include <mutex>
+#include <sstream>
+
+#include "kernel_src.inc"  // SE_PRELUDE_SRC, SE_MARGOLUS_SRC (generated from csrc/kernels)
+
+namespace se::rt {
+
+std::string TileVariant::name() const {
+  return "se_tile_" + std::to_string(tw) + "x" + std::to_string(th) + "_k" + std::to_string(kmax);
+}
+
+// Tile shapes and fusion depths compiled into every rule-set module; the launcher and the
+// autotuner choose among them.  All use 256 threads.
+const std::vector<TileVariant>& tile_variants() {
+  static const std::vector<TileVariant> v = {
+      {128, 64, 1, 256}, {256, 32, 1, 256}, {128, 32, 1, 256},  {128, 64, 2, 256},
+      {128, 64, 4, 256}, {128, 64, 8, 256}, {128, 128, 8, 256}, {128, 128, 16, 256},
+      {256, 64, 4, 256}, {64, 64, 4, 256},
+  };
+  return v;
+}
+
+std::string kernel_source(const std::string& generated_rules) {
+  std::ostringstream o;
+  o << SE_PRELUDE_SRC << "\n" << generated_rules << "\n" << SE_MARGOLUS_SRC << "\n";
+  for (const TileVariant& t : tile_variants()) {
+    o << "extern \"C\" __global__ void __launch_bounds__(" << t.nt << ") " << t.name()
+      << "(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W, int H, int f0, int k) {\n"
+      << "  se_tile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
+      << ">(src, dst, W, H, f0, k);\n}\n";
+  }
+  return o.str();
+}
+
+namespace {
+
+std::string cache_dir() {
+  if (const char* d = getenv("SE_CACHE_DIR")) return d;
+  if (const char* x = getenv("XDG_CACHE_HOME")) return std::string(x) + "/sandengine_gb300";
+  if (const char* h = getenv("HOME")) return std::string(h) + "/.cache/sandengine_gb300";
+  return "";
+}
+
+std::string hex_digest(const std::string& s) {
+  // FNV-1a 64 twice with different offsets: a cache key, not a security boundary.
+  uint64_t a = 1469598103934665603ull, b = 1099511628211ull * 7ull + 13ull;
+  for (unsigned char c : s) {
+    a = (a ^ c) * 1099511628211ull;
+    b = (b ^ c) * 0x100000001b3ull + 0x9e3779b97f4a7c15ull;
+  }
+  char buf[40];
+  snprintf(buf, sizeof buf, "%016llx%016llx", (unsigned long long)a, (unsigned long long)b);
+  return buf;
+}
+
+const std::vector<std::string>& nvrtc_options() {
+  static const std::vector<std::string> o = {"-arch=sm_103a", "--std=c++17", "--fmad=false", "-lineinfo",
+                                             "--extra-device-vectorization"};
+  return o;
+}
+
+std::mutex g_cache_mu;
+
+}  // namespace
+
+bool compile_cubin(const std::string& src, std::string* cubin, std::string* log) {
+  int maj = 0, min = 0;
+  nvrtcVersion(&maj, &min);
+  std::string key_src = src + "\n//nvrtc " + std::to_string(maj) + "." + std::to_string(min);
+  for (auto& o : nvrtc_options()) key_src += "\n//" + o;
+  const std::string key = hex_digest(key_src);
+  const std::string dir = cache_dir();
+  const std::string path = dir.empty() ? "" : dir + "/" + key + ".cubin";
+  {
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    if (!path.empty()) {
+      std::ifstream f(path, std::ios::binary);
+      if (f) {
+        std::stringstream ss;
+        ss << f.rdbuf();
+        *cubin = ss.str();
+        if (!cubin->empty()) return true;
+      }
+    }
+  }
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), "sandengine_rules.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+    *log = "nvrtcCreateProgram failed";
+    return false;
+  }
+  std::vector<const char*> opts;
+  for (auto& o : nvrtc_options()) opts.push_back(o.c_str());
+  nvrtcResult rc = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
+  size_t lsz = 0;
+  nvrtcGetProgramLogSize(prog, &lsz);
+  std::string lg(lsz, '\0');
+  if (lsz) nvrtcGetProgramLog(prog, lg.data());
+  if (rc != NVRTC_SUCCESS) {
+    *log = std::string(nvrtcGetErrorString(rc)) + "\n" + lg;
+    nvrtcDestroyProgram(&prog);
+    return false;
+  }
+  size_t csz = 0;
+  nvrtcGetCUBINSize(prog, &csz);
+  cubin->assign(csz, '\0');
+  nvrtcGetCUBIN(prog, cubin->data());
+  nvrtcDestroyProgram(&prog);
+  if (!path.empty()) {
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    std::string cmd_dir = dir;
+    // mkdir -p
+    for (size_t i = 1; i <= cmd_dir.size(); ++i)
+      if (i == cmd_dir.size() || cmd_dir[i] == '/') mkdir(cmd_dir.substr(0, i).c_str(), 0755);
+    std::string tmp = path + ".tmp" + std::to_string(getpid());
+    std::ofstream f(tmp, std::ios::binary);
+    if (f) {
+      f.write(cubin->data(), (std::streamsize)cubin->size());
+      f.close();
+      rename(tmp.c_str(), path.c_str());
+    }
+  }
+  return true;
+}
+
+Module::~Module() {
+  if (lib) cudaLibraryUnload(lib);
+}
+
+bool Module::load(const std::string& cubin, std::string* err) {
+  cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) {
+    *err = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
+    lib = nullptr;
+    return false;
+  }
+  std::vector<std::string> names = {"se_edit"};
+  for (auto& t : tile_variants()) names.push_back(t.name());
+  for (auto& n : names) {
+    cudaKernel_t k;
+    e = cudaLibraryGetKernel(&k, lib, n.c_str());
+    if (e != cudaSuccess) {
+      *err = "cudaLibraryGetKernel(" + n + "): " + cudaGetErrorString(e);
+      return false;
+    }
+    kernels[n] = k;
+  }
+  for (auto& t : tile_variants()) {
+    e = cudaFuncSetAttribute((const void*)kernels[t.name()], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)t.smem_bytes());
+    if (e != cudaSuccess) {
+      *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+      return false;
+    }
+  }
+  return true;
+}
+
+cudaKernel_t Module::get(const std::string& name) const {
+  auto it = kernels.find(name);
+  return it == kernels.end() ? nullptr : it->second;
+}
+
+}  // namespace se::rt

@@ -1,0 +1,37 @@
+// NVRTC compilation of a rule set's kernels for sm_103a, with an on-disk cubin cache, and
+// loading through the CUDA runtime's library API (no link-time dependency on libcuda).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+namespace se::rt {
+
+// A tile-kernel instantiation: TW x TH output cells, up to KMAX frames per launch.
+struct TileVariant {
+  int tw, th, kmax, nt;
+  std::string name() const;
+  int halo_x() const { return ((kmax + 3) / 4) * 4; }
+  int halo_y() const { return kmax; }
+  size_t smem_bytes() const { return (size_t)(tw + 2 * halo_x()) * (size_t)(th + 2 * halo_y()); }
+};
+const std::vector<TileVariant>& tile_variants();
+
+// Full device source: prelude + generated rules + kernel template + instantiations.
+std::string kernel_source(const std::string& generated_rules);
+
+// Compiles `src` to an sm_103a cubin (cached by content hash).  No GPU needed.
+bool compile_cubin(const std::string& src, std::string* cubin, std::string* log);
+
+struct Module {
+  cudaLibrary_t lib = nullptr;
+  std::map<std::string, cudaKernel_t> kernels;
+  ~Module();
+  bool load(const std::string& cubin, std::string* err);
+  cudaKernel_t get(const std::string& name) const;
+};
+
+}  // namespace se::rt

@@ -1,0 +1,150 @@
+"""One simulated world, mirroring sandengine-core's ``Simulation``
+(sandengine-core/src/simulation.rs:97-253).
+
+    sim = Simulation(ruleset, (width, height))     # Simulation::new, all EMPTY, frame 0
+    sim.modifications.append(SimModification(...))
+    sim.run()                                      # Simulation::run: frame += 1, one step,
+                                                   #   mods applied, list cleared
+    sim.params.frame                               # Params.frame
+
+Extensions over the reference: ``run_frames(n, mods)`` advances n frames in one call
+(fused launches), ``grid`` reads/writes the cells as a numpy array, and ``digest()`` /
+``histogram()`` check a world on the device.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from ._lib import SeModification, check, lib
+from .lang import Ruleset
+
+MODSHAPE_CIRCLE = 0  # simulation.rs:41
+MODSHAPE_SQUARE = 1  # simulation.rs:42
+MAX_MODIFICATIONS = 256  # simulation.rs:43
+
+
+@dataclass
+class SimModification:
+    """simulation.rs:45-56 (the padding is implicit)."""
+    position: Tuple[int, int] = (0, 0)
+    mod_shape: int = MODSHAPE_CIRCLE
+    mod_size: int = 0
+    mod_matID: int = 0
+
+
+def mods_to_c(mods: Sequence[SimModification]):
+    arr = (SeModification * max(1, len(mods)))()
+    for i, m in enumerate(mods):
+        arr[i].position[0], arr[i].position[1] = int(m.position[0]), int(m.position[1])
+        arr[i].mod_shape, arr[i].mod_size, arr[i].mod_matID = int(m.mod_shape), int(m.mod_size), int(m.mod_matID)
+    return arr
+
+
+class Params:
+    """The part of simulation.rs:67-79 that drives the grid: the frame counter."""
+
+    def __init__(self, sim: "Simulation"):
+        self._sim = sim
+
+    @property
+    def frame(self) -> int:
+        f = ctypes.c_int32(0)
+        check(lib().se_world_get_frame(self._sim._h, ctypes.byref(f)))
+        return f.value
+
+    @frame.setter
+    def frame(self, value: int) -> None:
+        check(lib().se_world_set_frame(self._sim._h, int(value)))
+
+
+class Simulation:
+    def __init__(self, ruleset: Ruleset, size: Tuple[int, int], steps_per_launch: int = 0):
+        self.ruleset = ruleset
+        self.size = (int(size[0]), int(size[1]))
+        h = ctypes.c_void_p()
+        check(lib().se_world_create(ruleset.handle, self.size[0], self.size[1], ctypes.byref(h)))
+        self._h = h
+        self.params = Params(self)
+        self.modifications: List[SimModification] = []
+        if steps_per_launch:
+            self.set_steps_per_launch(steps_per_launch)
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            lib().se_world_destroy(h)
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def set_steps_per_launch(self, k: int) -> None:
+        check(lib().se_world_set_steps_per_launch(self._h, int(k)))
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        check(lib().se_world_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def set_stream(self, stream_ptr: Optional[int]) -> None:
+        check(lib().se_world_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def run(self) -> None:
+        """Simulation::run (simulation.rs:195-253)."""
+        self.run_frames(1, self.modifications)
+        self.modifications.clear()
+
+    def run_frames(self, nframes: int, mods: Sequence[SimModification] = ()) -> None:
+        """Advance ``nframes`` frames; ``mods`` apply to the first one."""
+        arr = mods_to_c(mods)
+        check(lib().se_world_step(self._h, int(nframes), arr if len(mods) else None, len(mods)))
+
+    def synchronize(self) -> None:
+        check(lib().se_world_synchronize(self._h))
+
+    @property
+    def grid(self) -> np.ndarray:
+        w, h = self.size
+        out = np.empty((h, w), dtype=np.uint32)
+        check(lib().se_world_get_grid(self._h, out.ctypes.data, out.size))
+        return out
+
+    @grid.setter
+    def grid(self, cells: np.ndarray) -> None:
+        w, h = self.size
+        a = np.ascontiguousarray(cells, dtype=np.uint32)
+        if a.shape != (h, w):
+            raise ValueError(f"grid must have shape {(h, w)}, got {a.shape}")
+        check(lib().se_world_set_grid(self._h, a.ctypes.data, a.size))
+
+    def device_grid_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        check(lib().se_world_device_grid(self._h, ctypes.byref(p)))
+        return p.value or 0
+
+    def digest(self) -> int:
+        d = ctypes.c_uint64(0)
+        check(lib().se_world_digest(self._h, ctypes.byref(d)))
+        return d.value
+
+    def histogram(self, nbins: Optional[int] = None) -> np.ndarray:
+        n = nbins or (self.ruleset.num_materials + 1)
+        out = np.zeros(n, dtype=np.uint64)
+        check(lib().se_world_histogram(self._h, out.ctypes.data, n))
+        return out
+
+
+def grid_digest(grid: np.ndarray) -> int:
+    """Host computation of Simulation.digest() for a (H, W) uint32 grid."""
+    g = np.ascontiguousarray(grid, dtype=np.uint32).ravel().astype(np.uint64)
+    z = (np.arange(g.size, dtype=np.uint64) << np.uint64(32)) | g
+    with np.errstate(over="ignore"):
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return int(z.sum(dtype=np.uint64))

@@ -1,0 +1,106 @@
+"""CPU emulation of the JIT device code.  TEST INFRASTRUCTURE ONLY.
+
+Compiles the exact source handed to NVRTC (Ruleset.kernel_source) with g++ against
+cuda_host_shim.hpp and runs the tile kernels with one thread per CTA (see the shim's
+header) and the edit kernel thread by thread.
+"""
+import ctypes
+import hashlib
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle", "_build")
+
+VARIANTS = [(128, 64, 1), (256, 32, 1), (128, 32, 1), (128, 64, 2), (128, 64, 4), (128, 64, 8),
+            (128, 128, 8), (128, 128, 16), (256, 64, 4), (64, 64, 4)]
+
+DRIVER = r'''
+alignas(16) uint8_t se_smem[1 << 20];
+#define EMU_TILE(TW, TH, K) \
+extern "C" void emu_tile_##TW##x##TH##_k##K(const uint32_t* src, uint32_t* dst, int W, int H, int f0, int k) { \
+  blockDim.x = 1; threadIdx.x = 0; \
+  for (unsigned by = 0; by < (unsigned)((H + TH - 1) / TH); ++by) \
+    for (unsigned bx = 0; bx < (unsigned)((W + TW - 1) / TW); ++bx) { \
+      blockIdx.x = bx; blockIdx.y = by; \
+      se_tile_impl<TW, TH, K, 1>(src, dst, W, H, f0, k); \
+    } \
+}
+%s
+extern "C" void emu_edit(uint32_t* grid, int W, int H, int nmods, long long total, const void* params) {
+  const SeEditParams& p = *reinterpret_cast<const SeEditParams*>(params);
+  blockDim.x = 256;
+  for (long long t = 0; t < total; ++t) {
+    blockIdx.x = (unsigned)(t / 256);
+    threadIdx.x = (unsigned)(t % 256);
+    se_edit(grid, W, H, nmods, total, p);
+  }
+}
+'''
+
+
+class Emu:
+    def __init__(self, ruleset):
+        src = ruleset.kernel_source
+        tiles = "\n".join(f"EMU_TILE({a}, {b}, {c})" for a, b, c in VARIANTS)
+        code = '#include "cuda_host_shim.hpp"\n' + src + DRIVER.replace('%s', tiles)
+        key = hashlib.sha256((code + open(os.path.join(HERE, "cuda_host_shim.hpp")).read()).encode()).hexdigest()[:16]
+        d = os.path.join(OUT, "emu_" + key)
+        so = os.path.join(d, "emu.so")
+        if not os.path.exists(so):
+            os.makedirs(d, exist_ok=True)
+            cpp = os.path.join(d, "emu.cpp")
+            with open(cpp, "w") as f:
+                f.write(code)
+            tmp = so + f".tmp{os.getpid()}"
+            r = subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-ffp-contract=off",
+                                "-fno-strict-aliasing", "-w", f"-I{HERE}", cpp, "-o", tmp],
+                               capture_output=True, text=True)
+            if r.returncode:
+                raise RuntimeError(r.stderr[-4000:])
+            os.replace(tmp, so)
+        self.lib = ctypes.CDLL(so)
+        self.nmat = ruleset.num_materials
+
+    def tiles(self, src: np.ndarray, f0: int, k: int, variant=None) -> np.ndarray:
+        """k frames (counters f0..f0+k-1) with one launch of the tile kernel."""
+        if variant is None:
+            variant = min((v for v in VARIANTS if v[2] >= k), key=lambda v: v[2])
+        fn = getattr(self.lib, "emu_tile_%dx%d_k%d" % variant)
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        H, W = src.shape
+        dst = np.zeros_like(src)
+        fn(src.ctypes.data, dst.ctypes.data, W, H, f0, k)
+        return dst
+
+    def edit(self, grid: np.ndarray, mods) -> None:
+        """The edit pass in place; host-side preparation as in runtime/engine.cpp."""
+        H, W = grid.shape
+        buf = np.zeros(14352 // 4, dtype=np.int32)
+        m = buf[:2048].reshape(256, 8)
+        box = buf[2048:3072].reshape(256, 4)
+        start = buf[3072:3072 + 514].view(np.int64)
+        live = []
+        for mod in mods[:256]:
+            if mod[3] == 0:
+                break
+            live.append(mod)
+        total = 0
+        for i, (px, py, shape, size, mat) in enumerate(live):
+            m[i, :5] = (px, py, shape, size, mat if 0 <= mat < self.nmat else 1)
+            r = abs(size)
+            normal = r < (1 << 22) and abs(px) < (1 << 30) and abs(py) < (1 << 30)
+            x0, y0, x1, y1 = 0, 0, W - 1, H - 1
+            if normal:
+                x0, x1, y0, y1 = max(0, px - r), min(W - 1, px + r), max(0, py - r), min(H - 1, py + r)
+            start[i] = total
+            if x1 >= x0 and y1 >= y0:
+                box[i] = (x0, y0, x1, y1)
+                total += (x1 - x0 + 1) * (y1 - y0 + 1)
+        start[len(live)] = total
+        if total:
+            self.lib.emu_edit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_longlong, ctypes.c_void_p]
+            self.lib.emu_edit(grid.ctypes.data, W, H, len(live), total, buf.ctypes.data)

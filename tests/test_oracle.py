@@ -1,0 +1,140 @@
+"""The oracle pinned: its front end against the reference's generated files, its error
+kinds against the reference's tests, its port against the reference's own compute
+shader (compiled on the CPU) and against the recorded per-frame digests."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import frontend as fe
+from oracle.build import Port, Ref, reference_root
+from sandengine_gb300.simulation import grid_digest
+from tests.conftest import GOLDEN
+from tests.golden.cases import CASES
+from tests.golden.yaml_corpus import CORPUS
+
+
+def _gen_golden():
+    with open(os.path.join(GOLDEN, "reference_gen.json")) as f:
+        return json.load(f)
+
+
+def test_frontend_reproduces_reference_generated_glsl(rulesets):
+    """data/materials.yaml -> gen/materials.glsl and gen/rules.glsl, byte for byte."""
+    mat, rules = fe.create_glsl(fe.parse_string(rulesets["reference"]))
+    gold = _gen_golden()
+    for name, text in (("materials.glsl", mat), ("rules.glsl", rules)):
+        data = text.encode()
+        assert len(data) == gold[name]["bytes"]
+        assert hashlib.sha256(data).hexdigest() == gold[name]["sha256"]
+
+
+@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout")
+def test_flattener_reproduces_reference_falling_sand():
+    from oracle.build import reference_shader_text
+    with open(os.path.join(GOLDEN, "reference_materials.yaml")) as f:
+        text = reference_shader_text(f.read(), reference_root())
+    gold = _gen_golden()["falling_sand.glsl"]
+    assert hashlib.sha256(text.encode()).hexdigest() == gold["sha256"]
+
+
+@pytest.mark.parametrize("name, kind", [
+    # the reference's tests (tests/test_sandengine-lang.rs) and what its code returns for
+    # their inputs: missing sections, a numeric rule name checked after the missing
+    # `types`, a missing field, and a do-string the do-parser does not recognise.
+    ("missing_rules", "MissingField"),
+    ("missing_types", "MissingField"),
+    ("missing_materials", "MissingField"),
+    ("number_rule_name_without_types", "MissingField"),
+    ("number_rule_name", "InvalidType"),
+    ("missing_if", "MissingField"),
+    ("missing_color", "MissingField"),
+    ("unknown_type", "NotFound"),
+    ("function_call_do", "NotRecognized"),
+])
+def test_error_kinds_follow_reference_code(name, kind):
+    with pytest.raises(fe.ParseError) as e:
+        fe.parse_string(CORPUS[name])
+    assert e.value.kind == kind
+    assert f"({kind})" in str(e.value)
+
+
+def test_hash43_lanes_and_mirror_threshold(ports):
+    """hash43 lanes equal RN(float(u)) * 2^-32 of the integer lanes, and the mirror test
+    rand.x < 0.5 equals lane < 2^31 - 64 (the lane value the CUDA kernel compares)."""
+    port = ports["four_materials"]
+
+    def lanes(x, y, f):
+        v = (x * 461 + y * 2131 + f * 4541161) & 0xFFFFFFFF
+        out = []
+        for m in (213, 2131, 21313, 213132):
+            h = (v * m) & 0xFFFFFFFF
+            h ^= h >> 16
+            h = (h * 0x7FEB352D) & 0xFFFFFFFF
+            h ^= h >> 15
+            h = (h * 0x846CA68B) & 0xFFFFFFFF
+            h ^= h >> 16
+            out.append(h)
+        return out
+
+    rng = np.random.default_rng(1)
+    for _ in range(500):
+        x, y, f = (int(v) for v in rng.integers(-3, 5000, 3))
+        got = port.hash43(x, y, f)
+        ls = lanes(x, y, f)
+        want = np.array([np.float32(np.float32(h) * np.float32(2.0 ** -32)) for h in ls], dtype=np.float32)
+        assert np.array_equal(got, want)
+        assert (got[0] < np.float32(0.5)) == (ls[0] < 0x7FFFFFC0)
+    for u in (0x7FFFFFBF, 0x7FFFFFC0, 0x7FFFFFC1, 0x80000000):
+        assert (np.float32(u) * np.float32(2.0 ** -32) < np.float32(0.5)) == (u < 0x7FFFFFC0)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+def test_port_matches_reference_digests(case):
+    with open(os.path.join(GOLDEN, "grids.json")) as f:
+        gold = json.load(f)[case.name]["digests"]
+    port = Port(case.ruleset_text())
+    g = case.initial_grid()
+    for i in range(case.frames):
+        port.step(g, case.frame0 + 1 + i, case.mods_at(i), nthreads=4)
+        assert grid_digest(g) == int(gold[i]), f"frame {case.frame0 + 1 + i}"
+
+
+@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout")
+@pytest.mark.parametrize("name", ["reference", "four_materials", "twelve_materials"])
+def test_port_matches_reference_shader(rulesets, name):
+    """Random worlds with unknown ids, WALL/NULL cells and overlapping edits of every
+    kind (unknown material, size 0 terminator, negative position, squares)."""
+    text = rulesets[name]
+    P, R = Port(text), Ref(text)
+    rng = np.random.default_rng(7)
+    for H, W in ((37, 50), (16, 16), (5, 9)):
+        g = rng.integers(0, P.num_materials + 3, size=(H, W)).astype(np.uint32)
+        g[rng.random((H, W)) < 0.4] = 0
+        gp, gr = g.copy(), g.copy()
+        for f in range(2, 90):
+            mods = None
+            if f % 5 == 0:
+                mods = [(int(rng.integers(-5, W + 5)), int(rng.integers(-5, H + 5)), int(rng.integers(0, 3)),
+                         int(rng.integers(-2, 8)), int(rng.integers(0, P.num_materials + 2))) for _ in range(6)]
+            P.step(gp, f, mods)
+            gr = R.step(gr, f, mods, nthreads=4)
+            assert np.array_equal(gp, gr), f"{name} {H}x{W} frame {f}"
+
+
+@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout")
+def test_port_edit_pass_extreme_mods(rulesets):
+    """Mods far outside the grid, huge radii and positions whose difference wraps."""
+    text = rulesets["four_materials"]
+    P, R = Port(text), Ref(text)
+    g = np.zeros((20, 24), dtype=np.uint32)
+    g[5:15, 5:15] = 3
+    mods = [(-2**31 + 3, 4, 1, 2**31 - 1, 4), (12, 10, 0, 2**23, 5), (2**31 - 1, -2**31, 0, 7, 3),
+            (3, 3, 1, -4, 4), (10, 10, 0, 3, 1)]
+    for f in (2, 3, 6):
+        gp, gr = g.copy(), g.copy()
+        P.step(gp, f, mods)
+        gr = R.step(gr, f, mods)
+        assert np.array_equal(gp, gr)
