@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Benchmark of sandengine's Margolus grid update on GB300.
+
+Workload (default, the 16384^2 world): 16384 x 16384 cells (u32 ids, 1 GiB per buffer),
+the bundled twelve-material rule set (fire ignites wood p=1/16 and burns out p=1/32, acid
+eats stone p=1/8, lava, water, steam, ...), seed-2 fill in 64x64 material patches.  One
+step = 60 frames whose first frame carries 32 circle edits (radius 8-64, uniform
+positions, EMPTY or sand), i.e. one edit period.  Metric: cell-updates/s (one cell
+advanced one frame = one update).  Inputs are larger than L2 (129 MB), so no flush is
+needed between steps.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+                    [--workload world16384|world4096|world256] [--k FRAMES_PER_LAUNCH]
+
+--impl reference times the reference's own compute shader compiled for the CPU
+(oracle/_ref, the reference's shaders/compute/falling_sand.glsl with the rule set's
+generated GLSL) on all host cores, on a bounded band of the same world; without that
+build it times the oracle port.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FRAMES_PER_STEP = 60
+EDITS_PER_STEP = 32
+METRIC = "cell-updates/s (% HBM roofline); p50/p99 batched vs plain launch, bit-exact"
+UNIT = "cell-updates/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="world16384",
+                    choices=["world16384", "world8192", "world4096", "world256"])
+    ap.add_argument("--k", type=int, default=0, help="frames per launch (0 = autotuned)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    from sandengine_gb300 import workloads as wl
+    if name == "world16384":
+        return dict(name="world16384", ruleset="twelve_materials", size=16384,
+                    grid=lambda: wl.world_16384(2), edit_mats=[0, 3], fill="seed-2 64x64 patches")
+    if name == "world8192":  # the same world family at 1/4 size (ncu captures)
+        return dict(name="world8192", ruleset="twelve_materials", size=8192,
+                    grid=lambda: wl.world_16384(2, 8192), edit_mats=[0, 3], fill="seed-2 64x64 patches")
+    if name == "world4096":
+        return dict(name="world4096", ruleset="four_materials", size=4096,
+                    grid=lambda: wl.world_4096(1), edit_mats=[0, 3], fill="seed-1 iid 0.6/0.2/0.15/0.05")
+    return dict(name="world256", ruleset="four_materials", size=256,
+                grid=lambda: wl.world_256(0), edit_mats=[0, 3], fill="seed-0 iid 0.6/0.2/0.15/0.05")
+
+
+def step_mods(se, wl, size, r, mats):
+    raw = wl.circle_edits(size, size, 2, r, EDITS_PER_STEP, mats)
+    return [se.SimModification((m[0], m[1]), m[2], m[3], m[4]) for m in raw]
+
+
+def load_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(k, workload_name):
+    """DRAM bytes per tile-kernel launch from the committed ncu summary, if it covers this k."""
+    p = os.path.join(ROOT, "profiles", "tile_kernel_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    vals = {}
+    for line in open(p):
+        if "=" in line and not line.startswith("#"):
+            a, b = line.strip().split("=", 1)
+            vals[a.strip()] = b.strip()
+    try:
+        if int(vals.get("k", -1)) == k and vals.get("workload") == workload_name:
+            return float(vals["dram_bytes_per_launch"])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.out.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                maxs.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": max(maxs) if maxs else None,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def cpu_info():
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                model = line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return os.cpu_count() or 1, model
+
+
+def cpu_rate(W, wl_spec, seconds, prefer_reference=True):
+    """Cell-updates/s of the CPU implementation on a band of the workload's world.
+    Returns (rate, kind, cores, sample)."""
+    from sandengine_gb300 import workloads as wl
+    from oracle.build import Port, Ref
+    cores, model = cpu_info()
+    text = wl.ruleset_text(wl_spec["ruleset"])
+    full = wl_spec["grid"]()
+    kind = "port"
+    ref = None
+    if prefer_reference:
+        try:
+            ref = Ref(text)
+            kind = "reference"
+        except Exception:
+            ref = None
+    # band height giving ~0.5 s per frame, from a 16-row probe
+    probe = np.ascontiguousarray(full[:16])
+    port = None if ref else Port(text)
+
+    def run_band(band, frames):
+        t0 = time.perf_counter()
+        if ref:
+            tot = 0.0
+            for f in range(frames):
+                tot += ref.time_rows(band, 2 + f, 0, band.shape[0], cores)
+            return tot
+        g = band.copy()
+        port.run(g, 1, frames, None, cores)
+        return time.perf_counter() - t0
+
+    t = run_band(probe, 1)
+    rows = int(max(16, min(full.shape[0], 16 * 0.5 / max(t, 1e-6))))
+    band = np.ascontiguousarray(full[:rows])
+    t1 = run_band(band, 1)
+    frames = max(1, int(seconds / max(t1, 1e-6)))
+    secs = run_band(band, frames)
+    rate = band.size * frames / secs
+    sample = (f"{wl_spec['name']} rows 0-{rows - 1} ({W} x {rows} band of the seeded world), {frames} frame(s), "
+              f"{secs:.1f} s on {cores} threads ({model})")
+    return rate, kind, cores, sample
+
+
+def run_ours(args, rep):
+    import torch
+    import sandengine_gb300 as se
+    from sandengine_gb300 import workloads as wl
+
+    spec = workload(args.workload)
+    W = H = spec["size"]
+    rs = se.parse_string(wl.ruleset_text(spec["ruleset"]))
+    grid0 = spec["grid"]()
+    sim = se.Simulation(rs, (W, H))
+    sim.grid = grid0
+    sim.params.frame = 1
+    if args.k:
+        sim.set_steps_per_launch(args.k)
+        k = args.k
+    else:
+        k = sim.autotune(3)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    mods = [step_mods(se, wl, W, r, spec["edit_mats"]) for r in range(args.warmup + args.steps)]
+
+    for r in range(args.warmup):
+        sim.run_frames(FRAMES_PER_STEP, mods[r])
+    sim.synchronize()
+
+    sim.set_timing(True)
+    sim.read_timing()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rep.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        start.record(stream)
+        for r in range(args.steps):
+            sim.run_frames(FRAMES_PER_STEP, mods[args.warmup + r])
+        end.record(stream)
+        torch.cuda.synchronize()
+    rep.barrier()
+    ms = start.elapsed_time(end)
+    timing = sim.read_timing()
+    sim.set_timing(False)
+    ms_max = rep.max(ms)
+    updates = float(W) * H * FRAMES_PER_STEP * args.steps
+    value = rep.sum(updates) / (ms_max / 1e3)
+
+    # e2e through the public API with host buffers: per step the mods go host->device
+    # (kernel parameters) and the grid comes back into pinned host memory.
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((H, W), dtype=torch.int32, pin_memory=True)
+        from sandengine_gb300._lib import check, lib
+        rep.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for r in range(args.steps):
+            sim.run_frames(FRAMES_PER_STEP, mods[args.warmup + r])
+            check(lib().se_world_get_grid_async(sim.handle, host.data_ptr(), W * H))
+        sim.synchronize()
+        e2e_s = rep.max(time.perf_counter() - t0)
+        e2e = {"value": rep.sum(updates) / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": EDITS_PER_STEP * 32, "d2h_bytes_per_step": W * H * 4}
+
+    peak, peak_src = load_peak()
+    launches = timing["launches"]
+    kernel_ms = timing["kernel_ms"]
+    alg_bytes_per_launch = 8.0 * timing["cells"] / max(launches, 1)
+    avg_launch_s = kernel_ms / max(launches, 1) / 1e3
+    achieved = alg_bytes_per_launch / avg_launch_s / 1e9 if launches else None
+    traffic = load_traffic(k, spec["name"])
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": rep.world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded splitmix64)",
+        "config": {"workload": f"{spec['name']}: {W}x{H} u32 cells, {spec['ruleset']} rule set, {spec['fill']}, "
+                               f"{FRAMES_PER_STEP} frames per step, {EDITS_PER_STEP} circle edits on the first",
+                   "frames_per_launch": k, "l2": "inputs larger than L2 (1 GiB per buffer)" if W >= 8192
+                   else "world fits in L2; no flush", "parallelism": f"replicas{rep.world_size}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": f"se_tile (k={k})", "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": alg_bytes_per_launch,
+                     "avg_launch_ms": avg_launch_s * 1e3, "kernel_share_of_step": kernel_ms / ms if ms else None},
+        "gpu_launches": launches + args.steps,
+        "clocks": clocks.summary(),
+    }
+    if e2e:
+        out["e2e"] = e2e
+    if rep.rank == 0 and rep.world_size == 1 and not args.no_cpu_baseline:
+        rate, kind, cores, sample = cpu_rate(W, spec, args.cpu_seconds)
+        out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+    return out
+
+
+def run_reference(args, rep):
+    if rep.rank != 0:
+        return None
+    spec = workload(args.workload)
+    W = spec["size"]
+    from sandengine_gb300 import workloads as wl
+    from oracle.build import Port, Ref
+    text = wl.ruleset_text(spec["ruleset"])
+    full = spec["grid"]()
+    cores, model = cpu_info()
+    try:
+        ref = Ref(text)
+        kind = "reference"
+    except Exception:
+        ref = None
+        kind = "port"
+    port = None if ref else Port(text)
+    rows = 64 if W >= 4096 else W
+    band = np.ascontiguousarray(full[:rows])
+
+    def one(f):
+        if ref:
+            return ref.time_rows(band, f, 0, rows, cores)
+        g = band.copy()
+        t0 = time.perf_counter()
+        port.run(g, f - 1, 1, None, cores)
+        return time.perf_counter() - t0
+
+    for i in range(args.warmup):
+        one(2 + i)
+    times = [one(2 + args.warmup + i) for i in range(args.steps)]
+    value = band.size * args.steps / sum(times)
+    sample = f"{spec['name']} rows 0-{rows - 1} ({W} x {rows} band), one frame per step, {cores} threads ({model})"
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": rep.world_size,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 texels (ids)",
+            "data": "synthetic (seeded splitmix64)",
+            "config": {"workload": f"{spec['name']}: {spec['ruleset']} rule set, {spec['fill']}; "
+                                   f"reference compute shader on the CPU, bounded band sample",
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse_args()
+    from sandengine_gb300.replicas import Replicas
+    rep = Replicas("nccl" if args.impl == "ours" else "gloo")
+    try:
+        out = run_ours(args, rep) if args.impl == "ours" else run_reference(args, rep)
+        if rep.rank == 0 and out is not None:
+            print(json.dumps(out), flush=True)
+    finally:
+        rep.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -103,8 +103,13 @@ void se_world_destroy(se_world* w);
 int se_world_set_stream(se_world* w, void* cuda_stream);
 int se_world_get_stream(se_world* w, void** cuda_stream);
 /* Fusion depth: frames advanced per launch when no edit intervenes (1 = one launch per
- * frame, like the reference; 0 = the library's tuned default). */
+ * frame, like the reference; 0 = chosen by the autotuner on the first multi-frame step). */
 int se_world_set_steps_per_launch(se_world* w, int k);
+/* Times every compiled tile shape and fusion depth on this world (`reps` launches each,
+ * reading the current grid into the spare buffer, so the world's state is unchanged) and
+ * keeps the fastest; *best_k gets the chosen frames per launch.  (No counterpart in the
+ * reference, which dispatches one frame at a time.) */
+int se_world_autotune(se_world* w, int reps, int* best_k);
 /* Replace / read the grid (width*height uint32, row-major) from host memory.  Both
  * synchronize the world's stream. */
 int se_world_set_grid(se_world* w, const uint32_t* cells, size_t count);
@@ -133,6 +138,15 @@ int se_world_digest(se_world* w, uint64_t* digest);
  * values >= nbins-1.  nbins in [1, 257].  Synchronizes the stream.  (No counterpart in the
  * reference: material-conservation checks.) */
 int se_world_histogram(se_world* w, uint64_t* counts, int nbins);
+/* Opt-in timing of the Margolus tile kernel: with enable != 0, every tile launch is
+ * bracketed by CUDA events on the world's stream.  se_world_read_timing synchronizes and
+ * returns, since the last read, the summed kernel time, the number of launches, the cell
+ * updates they performed (cells x frames) and the cells they read (one u32 read + one u32
+ * write each: the launch's algorithmic bytes are 8 x cells).  (No counterpart in the
+ * reference: roofline measurement.) */
+int se_world_set_timing(se_world* w, int enable);
+int se_world_read_timing(se_world* w, double* kernel_ms, long long* launches, long long* cell_frames,
+                         long long* cells);
 
 #ifdef __cplusplus
 }

@@ -170,6 +170,24 @@ class Ref:
         self.lib = ctypes.CDLL(build_ref(yaml_text))
         self.lib.ref_dispatch.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 3 + \
             [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        self.lib.ref_dispatch_rows.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int] * 3 + \
+            [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+
+    def time_rows(self, grid: np.ndarray, frame: int, y0: int, y1: int, nthreads: int) -> float:
+        """Seconds for the invocations of rows [y0, y1) of one dispatch over ``grid``."""
+        import time
+        H, W = grid.shape
+        tex_in = np.zeros((H, W, 4), dtype=np.float32)
+        tex_in[..., 0] = np.minimum(grid, (1 << 24) - 1).astype(np.float32)
+        out = np.zeros_like(tex_in)
+        light_in = np.zeros_like(tex_in)
+        light_out = np.zeros_like(tex_in)
+        color = np.zeros_like(tex_in)
+        t = time.perf_counter()
+        self.lib.ref_dispatch_rows(tex_in.ctypes.data, out.ctypes.data, color.ctypes.data,
+                                   light_in.ctypes.data, light_out.ctypes.data, W, H, frame, None, 0,
+                                   nthreads, y0, y1)
+        return time.perf_counter() - t
 
     def step(self, grid: np.ndarray, frame: int, mods=None, nthreads: int = 1,
              light: Optional[np.ndarray] = None, color: Optional[np.ndarray] = None) -> np.ndarray:

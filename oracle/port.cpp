@@ -51,6 +51,11 @@ static inline void swap(Cell& a, Cell& b) {
   b = t;
 }
 
+// The shader's uniforms that rule conditions may read (falling_sand.glsl:31-34); set by
+// port_step before any block is visited.
+static int frame = 0;
+static ivec2 simSize;
+
 #include "gen_rules.inc"
 
 namespace {
@@ -202,6 +207,8 @@ SE_EXPORT void port_step(uint32_t* grid, int W, int H, int frame, const void* mo
     return;
   }
   Grid G{grid, W, H};
+  ::frame = frame;
+  ::simSize = ivec2(W, H);
   const ivec2 off = margolus_offset(frame);
   const int nbx = (W - 1 + off.x) / 2 + 1;
   const int nby = (H - 1 + off.y) / 2 + 1;

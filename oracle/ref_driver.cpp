@@ -24,9 +24,21 @@ extern "C" {
 
 // in_data/out_data: RGBA32F W*H*4 (cell id in .r); in_light/out_light and out_color:
 // RGBA32F W*H*4.  mods: `nmods` 32-byte SimModification records (simulation.rs:45-56).
+SE_EXPORT void ref_dispatch_rows(const float* in_data, float* out_data, float* out_color,
+                                 const float* in_light, float* out_light, int W, int H, int frame_value,
+                                 const void* mods_raw, int nmods, int nthreads, int y0, int y1);
+
 SE_EXPORT void ref_dispatch(const float* in_data, float* out_data, float* out_color, const float* in_light,
                   float* out_light, int W, int H, int frame_value, const void* mods_raw,
                   int nmods, int nthreads) {
+  ref_dispatch_rows(in_data, out_data, out_color, in_light, out_light, W, H, frame_value, mods_raw, nmods,
+                    nthreads, 0, H);
+}
+
+// The invocations of rows [y0, y1) only (a bounded sample of a dispatch, for timing).
+SE_EXPORT void ref_dispatch_rows(const float* in_data, float* out_data, float* out_color,
+                                 const float* in_light, float* out_light, int W, int H, int frame_value,
+                                 const void* mods_raw, int nmods, int nthreads, int y0, int y1) {
   input_data = sampler2D{in_data, W, H};
   output_data = image2D{out_data, W, H};
   output_color = image2D{out_color, W, H};
@@ -56,7 +68,7 @@ SE_EXPORT void ref_dispatch(const float* in_data, float* out_data, float* out_co
   }
   if (nthreads <= 0) nthreads = 1;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
-  for (int y = 0; y < H; ++y)
+  for (int y = y0; y < y1; ++y)
     for (int x = 0; x < W; ++x) {
       gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
       glsl_main();

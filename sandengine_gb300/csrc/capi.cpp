@@ -276,3 +276,32 @@ SE_API int se_world_histogram(se_world* w, uint64_t* counts, int nbins) {
     return ret(w->w->histogram(reinterpret_cast<unsigned long long*>(counts), nbins));
   });
 }
+
+SE_API int se_world_autotune(se_world* w, int reps, int* best_k) {
+  return guard([&] {
+    if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
+    int k = 0;
+    se::rt::Status s = w->w->autotune(reps, &k);
+    if (!s.ok()) return ret(s);
+    w->w->steps_per_launch = 0;
+    if (best_k) *best_k = k;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_set_timing(se_world* w, int enable) {
+  return guard([&] {
+    if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
+    w->w->timing = enable != 0;
+    w->w->timed_used = 0;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_read_timing(se_world* w, double* kernel_ms, long long* launches, long long* cell_frames,
+                                long long* cells) {
+  return guard([&] {
+    if (!w || !kernel_ms || !launches || !cell_frames || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(w->w->timing_read(kernel_ms, launches, cell_frames, cells));
+  });
+}

@@ -39,11 +39,9 @@ __device__ __forceinline__ uint32_t se_norm(uint32_t v) { return v < (uint32_t)S
 // simulate() for the block with top-left cell (gx, gy) (falling_sand.glsl:72-114).
 // The caller has already skipped all-EMPTY blocks (:77-79).
 // rand.x < 0.5 <=> RN(float(h0)) < 2^31 <=> h0 < 2^31 - 64 (2^31 - 64 rounds to 2^31).
-__device__ __forceinline__ void se_block(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d, int gx, int gy,
-                                         int f, int W, int H) {
-  const uint32_t x = (uint32_t)gx * 461u + (uint32_t)gy * 2131u + (uint32_t)f * 4541161u;  // hash43
-  const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u),
-                 h3 = se_mix(x * 213132u);
+__device__ __forceinline__ void se_rules_hashed(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d, uint32_t h0,
+                                                uint32_t h1, uint32_t h2, uint32_t h3, int gx, int gy, int f,
+                                                int W, int H) {
   const bool mirror = h0 < 0x7fffffc0u;
   if (mirror) {
     se_swap(a, b);
@@ -60,13 +58,41 @@ __device__ __forceinline__ void se_block(uint32_t& a, uint32_t& b, uint32_t& c, 
     se_gen::apply_left(a, b, c, d, h0, h1, h2, h3, gx, gy, f, W, H);
 }
 
+// hash43(uvec3(origin, frame)) lanes (math.glsl:74-79), then the rules.
+__device__ __forceinline__ void se_block(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d, int gx, int gy,
+                                         int f, int W, int H) {
+  const uint32_t x = (uint32_t)gx * 461u + (uint32_t)gy * 2131u + (uint32_t)f * 4541161u;
+  const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u),
+                 h3 = se_mix(x * 213132u);
+  se_rules_hashed(a, b, c, d, h0, h1, h2, h3, gx, gy, f, W, H);
+}
+
+#ifdef SE_LUT
+// Fills the block transition table: entry i holds the four output ids (4 bits each) of
+// the block and hash intervals that se_gen::lut_index maps to i.  Keys naming an id >=
+// SE_NMAT never occur (cells are normalised on load) and keep their input.
+extern "C" __global__ void __launch_bounds__(256) se_build_lut(uint16_t* __restrict__ lut) {
+  se_gen::init_tables(threadIdx.x, blockDim.x);
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < SE_LUT_ENTRIES; i += gridDim.x * blockDim.x) {
+    uint32_t a, b, c, d, h0, h1, h2, h3;
+    se_gen::lut_decode(i, a, b, c, d, h0, h1, h2, h3);
+    if (a < SE_NMAT && b < SE_NMAT && c < SE_NMAT && d < SE_NMAT && (a | b | c | d) != 0u)
+      se_rules_hashed(a, b, c, d, h0, h1, h2, h3, 0, 0, 0, 0, 0);  // the rules read no position
+    lut[i] = (uint16_t)(a | (b << 4) | (c << 8) | (d << 12));
+  }
+}
+// Tables up to this size are copied into shared memory by each CTA.
+#define SE_LUT_SMEM_MAX_ENTRIES 16384u
+#endif
+
 // One step over the shared array: every block wholly inside it.  OX and ly0 are the
 // parities of the first block column / row in shared-array coordinates: a block's global
 // top-left cell is congruent to the frame's offset modulo 2, and the array starts at global
 // (gx0, gy0).  OX is compile-time so the block index split is a constant division.
 template <int SW, int SH, int OX, int NT>
 __device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int gy0, int f, int W, int H,
-                                             bool edge) {
+                                             bool edge, const uint16_t* __restrict__ lut) {
   constexpr int NBX = (SW - OX) / 2;
   const int nb = NBX * ((SH - ly0) / 2);
   for (int bi = threadIdx.x; bi < nb; bi += NT) {
@@ -76,7 +102,25 @@ __device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int 
     uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
     if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
     const int gx = gx0 + lx, gy = gy0 + ly;
+#ifdef SE_LUT
+    {
+      const uint32_t x = (uint32_t)gx * 461u + (uint32_t)gy * 2131u + (uint32_t)f * 4541161u;
+      const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u),
+                     h3 = se_mix(x * 213132u);
+      const uint32_t idx = se_gen::lut_index(a, b, c, d, h0, h1, h2, h3);
+#if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
+      const uint32_t o = lut[idx];  // shared-memory copy
+#else
+      const uint32_t o = __ldg(lut + idx);
+#endif
+      a = o & 15u;
+      b = (o >> 4) & 15u;
+      c = (o >> 8) & 15u;
+      d = o >> 12;
+    }
+#else
     se_block(a, b, c, d, gx, gy, f, W, H);
+#endif
     if (!edge) {
       p[0] = (uint8_t)a;
       p[1] = (uint8_t)b;
@@ -97,13 +141,21 @@ __device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int 
 // counters are f0, f0+1, ... (all >= 2; the host handles the frame-1 clear).
 template <int TW, int TH, int KMAX, int NT>
 __device__ __forceinline__ void se_tile_impl(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W,
-                                             int H, int f0, int k) {
+                                             int H, int f0, int k, const uint16_t* __restrict__ lut) {
   constexpr int HX = ((KMAX + 3) / 4) * 4, HY = KMAX;
   constexpr int SW = TW + 2 * HX, SH = TH + 2 * HY, WPR = SW / 4;
   static_assert(TW % 4 == 0, "tile width must be a multiple of 4");
   extern __shared__ __align__(16) uint8_t se_smem[];
   uint8_t* sm = se_smem;
   se_gen::init_tables(threadIdx.x, NT);
+#if defined(SE_LUT) && SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
+  {  // small tables live in shared memory, after the tile
+    uint16_t* slut = reinterpret_cast<uint16_t*>(se_smem + ((SW * SH + 15) & ~15));
+    for (uint32_t i = threadIdx.x; i < SE_LUT_ENTRIES / 2u; i += NT)
+      reinterpret_cast<uint32_t*>(slut)[i] = __ldg(reinterpret_cast<const uint32_t*>(lut) + i);
+    lut = slut;
+  }
+#endif
   const int X0 = blockIdx.x * TW, Y0 = blockIdx.y * TH;
   const int gx0 = X0 - HX, gy0 = Y0 - HY;
   const bool vec = (W & 3) == 0;
@@ -135,9 +187,9 @@ __device__ __forceinline__ void se_tile_impl(const uint32_t* __restrict__ src, u
     const int f = f0 + s;
     const int ly0 = (se_off_y(f) + gy0) & 1;  // gy0 = Y0 - HY is odd when HY is
     if (se_off_x(f) == 0)
-      se_tile_step<SW, SH, 0, NT>(sm, ly0, gx0, gy0, f, W, H, edge);
+      se_tile_step<SW, SH, 0, NT>(sm, ly0, gx0, gy0, f, W, H, edge, lut);
     else
-      se_tile_step<SW, SH, 1, NT>(sm, ly0, gx0, gy0, f, W, H, edge);
+      se_tile_step<SW, SH, 1, NT>(sm, ly0, gx0, gy0, f, W, H, edge, lut);
     __syncthreads();
   }
 

@@ -8,6 +8,7 @@ typedef int int32_t;
 typedef unsigned long long uint64_t;
 typedef long long int64_t;
 typedef unsigned char uint8_t;
+typedef unsigned short uint16_t;
 #endif
 
 // Material ids fixed by the rule language (materials.rs:52-78): EMPTY, NULL, WALL.

@@ -425,6 +425,8 @@ struct Gen {
   bool any_nan = false;
   bool used_density = false, used_type = false, used_color = false, used_emission = false;
   bool uses_lane[4] = {false, false, false, false};
+  std::set<uint64_t> bounds[4];  // threshold boundaries of rand.<lane> comparisons
+  std::string all_bodies;        // generated rule bodies (scanned for table eligibility)
   std::vector<std::vector<bool>> sets;   // material bit sets
   std::map<std::vector<bool>, int> set_index;
 
@@ -485,6 +487,13 @@ struct Gen {
     };
     uint64_t ge = first([&](float x) { return x >= c; });
     uint64_t gt = first([&](float x) { return x > c; });
+    // The comparison is constant between consecutive boundaries: remember them for the
+    // block transition table (see generate_cuda).
+    auto bound = [&](uint64_t T) {
+      if (T > 0 && T < (1ull << 32)) bounds[lane].insert(T);
+    };
+    if (o == "<" || o == ">=" || o == "==" || o == "!=") bound(ge);
+    if (o == "<=" || o == ">" || o == "==" || o == "!=") bound(gt);
     auto lit = [](uint64_t v) {
       char b[32];
       snprintf(b, sizeof b, "0x%08llxu", (unsigned long long)v);
@@ -912,6 +921,7 @@ struct Gen {
     if (P.peek().t != T::End) glsl_error(rule, "trailing text after function body");
     std::string code;
     stmt(*body, code, 1);
+    all_bodies += code;
     std::string sig = "__device__ __forceinline__ void rule_" + r.name + "(uint32_t& " + cell_names[0] +
                       ", uint32_t& " + cell_names[1] + ", uint32_t& " + cell_names[2] + ", uint32_t& " +
                       cell_names[3] + SE_RULE_TAIL_PARAMS + ")\n";
@@ -1054,8 +1064,62 @@ bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err) {
     o << "__device__ __forceinline__ void apply_mirrored" << params << " {\n" << mirrored << "}\n";
     o << "__device__ __forceinline__ void apply_right" << params << " {\n" << right << "}\n";
     o << "__device__ __forceinline__ void apply_left" << params << " {}\n";
+
+    // Block transition table.  When the rules read nothing but the four cells and rand
+    // lanes compared with constants, a block's update is a function of the four material
+    // ids and, per lane, the interval between consecutive comparison boundaries that the
+    // lane falls in (lane 0 also carries the mirror test, rand.x < 0.5 <=> h0 < 0x7fffffc0).
+    // The runtime fills the table once by running the rules above on one representative
+    // hash value per interval (se_build_lut); the tile kernel then replaces the rule
+    // evaluation by one lookup.
+    auto has_tok = [&](const std::string& tok) {
+      size_t p = 0;
+      while ((p = g.all_bodies.find(tok, p)) != std::string::npos) {
+        bool l = p == 0 || !(isalnum((unsigned char)g.all_bodies[p - 1]) || g.all_bodies[p - 1] == '_');
+        size_t e = p + tok.size();
+        bool r = e >= g.all_bodies.size() || !(isalnum((unsigned char)g.all_bodies[e]) || g.all_bodies[e] == '_');
+        if (l && r) return true;
+        p = e;
+      }
+      return false;
+    };
+    bool lut = g.nmat <= 16;
+    for (const char* t : {"pos_x", "pos_y", "frame", "sim_w", "sim_h", "se_randf"}) lut = lut && !has_tok(t);
+    g.bounds[0].insert(0x7fffffc0ull);
+    const int bits = g.nmat <= 2 ? 1 : g.nmat <= 4 ? 2 : g.nmat <= 8 ? 3 : 4;
+    uint64_t entries = 1ull << (4 * bits);
+    for (int l = 0; l < 4; ++l) entries *= g.bounds[l].size() + 1;
+    if (entries > (1ull << 24)) lut = false;
+    if (lut) {
+      o << "#define SE_LUT 1\n#define SE_LUT_BITS " << bits << "\n#define SE_LUT_ENTRIES " << entries << "u\n";
+      o << "__device__ __forceinline__ uint32_t lut_index(uint32_t a, uint32_t b, uint32_t c, uint32_t d, "
+           "uint32_t h0, uint32_t h1, uint32_t h2, uint32_t h3) {\n"
+        << "  uint32_t i = a | (b << " << bits << ") | (c << " << 2 * bits << ") | (d << " << 3 * bits << ");\n";
+      for (int l = 0; l < 4; ++l) {
+        if (g.bounds[l].empty()) continue;
+        o << "  i = i * " << g.bounds[l].size() + 1 << "u";
+        for (uint64_t T : g.bounds[l]) o << " + (h" << l << " >= " << T << "u)";
+        o << ";\n";
+      }
+      o << "  return i;\n}\n";
+      // decode: idx -> cells and one representative hash value per lane
+      o << "__device__ __forceinline__ void lut_decode(uint32_t i, uint32_t& a, uint32_t& b, uint32_t& c, "
+           "uint32_t& d, uint32_t& h0, uint32_t& h1, uint32_t& h2, uint32_t& h3) {\n"
+        << "  h0 = h1 = h2 = h3 = 0u;\n";
+      for (int l = 3; l >= 0; --l) {
+        if (g.bounds[l].empty()) continue;
+        const size_t n = g.bounds[l].size() + 1;
+        o << "  { const uint32_t reps[" << n << "] = {0u";
+        for (uint64_t T : g.bounds[l]) o << ", " << T << "u";
+        o << "}; h" << l << " = reps[i % " << n << "u]; i /= " << n << "u; }\n";
+      }
+      const uint32_t mask = (1u << bits) - 1;
+      o << "  a = i & " << mask << "u; b = (i >> " << bits << ") & " << mask << "u; c = (i >> " << 2 * bits
+        << ") & " << mask << "u; d = (i >> " << 3 * bits << ") & " << mask << "u;\n}\n";
+    }
     o << "}  // namespace se_gen\n";
     out->source = o.str();
+    out->lut_entries = lut ? entries : 0;
     out->num_materials = g.nmat;
     for (int i = 0; i < 4; ++i) out->uses_rand_lane[i] = g.uses_lane[i];
     return true;

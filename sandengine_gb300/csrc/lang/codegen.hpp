@@ -25,6 +25,10 @@ struct CudaRules {
   std::string source;  // device code, namespace se_gen (see kernels/margolus.cuh)
   int num_materials = 0;
   bool uses_rand_lane[4] = {false, false, false, false};
+  // Entries of the block transition table (u16 each), 0 when the rules need the direct
+  // evaluation path (they read positions / the frame, use rand as a number, or there are
+  // more than 16 materials).
+  unsigned long long lut_entries = 0;
 };
 
 bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err);

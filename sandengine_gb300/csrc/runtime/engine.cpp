@@ -35,12 +35,28 @@ Status Ruleset::ensure_loaded() {
   if (module) return Status::Ok();
   auto m = std::make_unique<Module>();
   std::string err;
-  if (!m->load(cubin, &err)) return {SE_ERR_CUDA, err};
+  if (!m->load(cubin, cuda.lut_entries, &err)) return {SE_ERR_CUDA, err};
+  if (cuda.lut_entries) {  // build the block transition table with the rules themselves
+    cudaError_t e = cudaMalloc(&d_lut, (size_t)cuda.lut_entries * sizeof(uint16_t));
+    if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    void* args[] = {(void*)&d_lut};
+    const unsigned blocks = (unsigned)std::min<unsigned long long>((cuda.lut_entries + 255) / 256, 4096);
+    SE_CUDA(cudaLaunchKernel((const void*)m->get("se_build_lut"), dim3(blocks), dim3(256), args, 0, nullptr));
+    SE_CUDA(cudaDeviceSynchronize());
+  }
   module = std::move(m);
   return Status::Ok();
 }
 
+Ruleset::~Ruleset() {
+  if (d_lut) cudaFree(d_lut);
+}
+
 World::~World() {
+  for (auto& t : timed) {
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+  }
   if (buf[0]) cudaFree(buf[0]);
   if (buf[1]) cudaFree(buf[1]);
   if (d_scratch) cudaFree(d_scratch);
@@ -73,7 +89,7 @@ Status World::create(std::shared_ptr<Ruleset> r, int w, int h) {
 
 int World::default_k() const {
   if (steps_per_launch > 0) return steps_per_launch;
-  return 1;
+  return fused ? fused->kmax : 1;
 }
 
 static const TileVariant* pick_variant(int k) {
@@ -83,17 +99,89 @@ static const TileVariant* pick_variant(int k) {
   return best;
 }
 
-Status World::launch_tiles(int f0, int k) {
-  const TileVariant* v = pick_variant(k);
-  if (!v) return {SE_ERR_INVALID_ARGUMENT, "no kernel variant for this many frames per launch"};
+Status World::autotune(int reps, int* best_k) {
+  if (reps < 1) reps = 1;
+  const int f0 = frame + 1 >= 2 ? frame + 1 : 2;  // trial frames never hit the frame-1 clear
+  struct Restore {
+    bool& flag;
+    bool saved;
+    ~Restore() { flag = saved; }
+  } restore{timing, timing};
+  timing = false;  // trials are not part of any measured region
+  cudaEvent_t a, b;
+  SE_CUDA(cudaEventCreate(&a));
+  SE_CUDA(cudaEventCreate(&b));
+  double best_multi = 0, best_one = 0;
+  const TileVariant *vm = nullptr, *v1 = nullptr;
+  for (const TileVariant& v : tile_variants()) {
+    Status s = launch_tiles(f0, v.kmax, &v, false);  // warm-up
+    if (!s.ok()) return s;
+    SE_CUDA(cudaEventRecord(a, stream));
+    for (int r = 0; r < reps; ++r) {
+      s = launch_tiles(f0, v.kmax, &v, false);
+      if (!s.ok()) return s;
+    }
+    SE_CUDA(cudaEventRecord(b, stream));
+    SE_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    SE_CUDA(cudaEventElapsedTime(&ms, a, b));
+    const double rate = (double)W * H * v.kmax * reps / (ms > 0 ? ms : 1e-6);  // cell updates per ms
+    if (v.kmax == 1 && rate > best_one) best_one = rate, v1 = &v;
+    if (rate > best_multi) best_multi = rate, vm = &v;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  fused = vm;
+  single = v1;
+  if (best_k) *best_k = vm ? vm->kmax : 1;
+  return Status::Ok();
+}
+
+Status World::launch_tiles(int f0, int k, const TileVariant* v, bool commit) {
+  if (!v || v->kmax < k) return {SE_ERR_INVALID_ARGUMENT, "no kernel variant for this many frames per launch"};
   cudaKernel_t kern = rs->module->get(v->name());
   const uint32_t* src = buf[cur];
   uint32_t* dst = buf[cur ^ 1];
   int Wv = W, Hv = H;
-  void* args[] = {(void*)&src, (void*)&dst, &Wv, &Hv, &f0, &k};
+  const uint16_t* lut = rs->d_lut;
+  void* args[] = {(void*)&src, (void*)&dst, &Wv, &Hv, &f0, &k, (void*)&lut};
   dim3 grid((unsigned)((W + v->tw - 1) / v->tw), (unsigned)((H + v->th - 1) / v->th));
-  SE_CUDA(cudaLaunchKernel((const void*)kern, grid, dim3((unsigned)v->nt), args, v->smem_bytes(), stream));
-  cur ^= 1;
+  const size_t smem = tile_smem_bytes(*v, rs->cuda.lut_entries);
+  Timed* t = nullptr;
+  if (timing) {
+    if (timed_used == timed.size()) {
+      Timed n{};
+      SE_CUDA(cudaEventCreate(&n.a));
+      SE_CUDA(cudaEventCreate(&n.b));
+      timed.push_back(n);
+    }
+    t = &timed[timed_used++];
+    t->cells = (long long)W * H;
+    t->frames = k;
+    SE_CUDA(cudaEventRecord(t->a, stream));
+  }
+  SE_CUDA(cudaLaunchKernel((const void*)kern, grid, dim3((unsigned)v->nt), args, smem, stream));
+  if (t) SE_CUDA(cudaEventRecord(t->b, stream));
+  if (commit) cur ^= 1;
+  return Status::Ok();
+}
+
+Status World::timing_read(double* ms, long long* launches, long long* cell_frames, long long* cells) {
+  SE_CUDA(cudaStreamSynchronize(stream));
+  double tot = 0;
+  long long cf = 0, c = 0;
+  for (size_t i = 0; i < timed_used; ++i) {
+    float m = 0;
+    SE_CUDA(cudaEventElapsedTime(&m, timed[i].a, timed[i].b));
+    tot += m;
+    cf += timed[i].cells * timed[i].frames;
+    c += timed[i].cells;
+  }
+  *ms = tot;
+  *launches = (long long)timed_used;
+  *cell_frames = cf;
+  *cells = c;
+  timed_used = 0;
   return Status::Ok();
 }
 
@@ -154,7 +242,18 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
   int nlive = 0;
   const int nseen = std::min(nmods, SE_MAX_MODIFICATIONS);  // simulation.rs:205
   while (nlive < nseen && mods[nlive].mod_size != 0) ++nlive;  // falling_sand.glsl:139-141
-  const int kdef = std::max(1, default_k());
+  const TileVariant* vmulti = nullptr;
+  if (steps_per_launch > 0) {
+    vmulti = pick_variant(steps_per_launch);
+  } else {
+    if (!fused && nframes - (nlive > 0 ? 1 : 0) >= 2) {
+      Status s = autotune(2, nullptr);
+      if (!s.ok()) return s;
+    }
+    vmulti = fused ? fused : pick_variant(1);
+  }
+  const TileVariant* vone = single ? single : pick_variant(1);
+  const int kdef = steps_per_launch > 0 ? steps_per_launch : vmulti->kmax;
   int i = 0;
   while (i < nframes) {
     const int f = frame + 1 + i;
@@ -164,7 +263,7 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
       continue;
     }
     if (i == 0 && nlive > 0) {
-      Status s = launch_tiles(f, 1);
+      Status s = launch_tiles(f, 1, vone);
       if (!s.ok()) return s;
       s = launch_edit(mods, nlive);
       if (!s.ok()) return s;
@@ -172,7 +271,7 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
       continue;
     }
     const int k = std::min(kdef, nframes - i);
-    Status s = launch_tiles(f, k);
+    Status s = launch_tiles(f, k, k == 1 ? vone : vmulti);
     if (!s.ok()) return s;
     i += k;
   }

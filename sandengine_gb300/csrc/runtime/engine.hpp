@@ -33,6 +33,8 @@ struct Ruleset {
   bool compiled = false;
   std::mutex mu;
   std::unique_ptr<Module> module;  // loaded on first use on a device
+  uint16_t* d_lut = nullptr;       // block transition table (when cuda.lut_entries > 0)
+  ~Ruleset();
   int num_materials() const { return (int)parsed.materials.size(); }
   Status compile();
   Status ensure_loaded();
@@ -55,14 +57,30 @@ struct World {
   int cur = 0;
   unsigned long long* d_scratch = nullptr;  // 258 words for digests and histograms
   cudaStream_t own_stream = nullptr, stream = nullptr;
-  int steps_per_launch = 0;  // 0: default
+  int steps_per_launch = 0;  // 0: chosen by the autotuner on the first multi-frame step
+  const TileVariant* fused = nullptr;   // variant for multi-frame launches
+  const TileVariant* single = nullptr;  // variant for one-frame launches (edit frames)
   ~World();
   Status create(std::shared_ptr<Ruleset> r, int w, int h);
   Status step(int nframes, const se_modification* mods, int nmods);
-  // k frames with counters f0.. from buf[cur] into buf[cur^1]
-  Status launch_tiles(int f0, int k);
+  // k frames with counters f0.. from buf[cur] into buf[cur^1]; commit=false leaves cur
+  // (the world's state) unchanged, for tuning trials.
+  Status launch_tiles(int f0, int k, const TileVariant* v, bool commit = true);
+  // Times every tile variant on this world (without changing it) and keeps the fastest
+  // multi-frame and one-frame variants.  *best_k gets the chosen frames per launch.
+  Status autotune(int reps, int* best_k);
   Status launch_edit(const se_modification* mods, int nlive);
   int default_k() const;
+  // Opt-in per-launch CUDA-event timing of the tile kernel (for roofline measurements).
+  bool timing = false;
+  struct Timed {
+    cudaEvent_t a, b;
+    long long cells;  // W*H of the launch
+    int frames;       // frames the launch advanced
+  };
+  std::vector<Timed> timed;
+  size_t timed_used = 0;
+  Status timing_read(double* ms, long long* launches, long long* cell_frames, long long* cells);
   Status digest(unsigned long long* out);
   Status histogram(unsigned long long* counts, int nbins);
 };

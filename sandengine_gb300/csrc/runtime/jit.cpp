@@ -35,9 +35,10 @@ std::string kernel_source(const std::string& generated_rules) {
   o << SE_PRELUDE_SRC << "\n" << generated_rules << "\n" << SE_MARGOLUS_SRC << "\n";
   for (const TileVariant& t : tile_variants()) {
     o << "extern \"C\" __global__ void __launch_bounds__(" << t.nt << ") " << t.name()
-      << "(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W, int H, int f0, int k) {\n"
+      << "(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W, int H, int f0, int k,"
+         " const uint16_t* __restrict__ lut) {\n"
       << "  se_tile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
-      << ">(src, dst, W, H, f0, k);\n}\n";
+      << ">(src, dst, W, H, f0, k, lut);\n}\n";
   }
   return o.str();
 }
@@ -136,7 +137,13 @@ Module::~Module() {
   if (lib) cudaLibraryUnload(lib);
 }
 
-bool Module::load(const std::string& cubin, std::string* err) {
+size_t tile_smem_bytes(const TileVariant& t, unsigned long long lut_entries) {
+  size_t b = (t.smem_bytes() + 15) & ~(size_t)15;
+  if (lut_entries && lut_entries <= kLutSmemMaxEntries) b += (size_t)lut_entries * 2;
+  return b;
+}
+
+bool Module::load(const std::string& cubin, unsigned long long lut_entries, std::string* err) {
   cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e != cudaSuccess) {
     *err = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
@@ -144,6 +151,7 @@ bool Module::load(const std::string& cubin, std::string* err) {
     return false;
   }
   std::vector<std::string> names = {"se_edit"};
+  if (lut_entries) names.push_back("se_build_lut");
   for (auto& t : tile_variants()) names.push_back(t.name());
   for (auto& n : names) {
     cudaKernel_t k;
@@ -156,7 +164,7 @@ bool Module::load(const std::string& cubin, std::string* err) {
   }
   for (auto& t : tile_variants()) {
     e = cudaFuncSetAttribute((const void*)kernels[t.name()], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)t.smem_bytes());
+                             (int)tile_smem_bytes(t, lut_entries));
     if (e != cudaSuccess) {
       *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
       return false;

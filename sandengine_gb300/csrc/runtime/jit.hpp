@@ -20,6 +20,13 @@ struct TileVariant {
 };
 const std::vector<TileVariant>& tile_variants();
 
+// Block transition tables up to this many entries are copied into shared memory by each
+// CTA (SE_LUT_SMEM_MAX_ENTRIES in kernels/margolus.cuh); larger ones are read from global
+// memory through the read-only cache.
+constexpr unsigned long long kLutSmemMaxEntries = 16384;
+// Dynamic shared memory of a tile launch: the u8 tile, then the table when it fits.
+size_t tile_smem_bytes(const TileVariant& t, unsigned long long lut_entries);
+
 // Full device source: prelude + generated rules + kernel template + instantiations.
 std::string kernel_source(const std::string& generated_rules);
 
@@ -30,7 +37,7 @@ struct Module {
   cudaLibrary_t lib = nullptr;
   std::map<std::string, cudaKernel_t> kernels;
   ~Module();
-  bool load(const std::string& cubin, std::string* err);
+  bool load(const std::string& cubin, unsigned long long lut_entries, std::string* err);
   cudaKernel_t get(const std::string& name) const;
 };
 

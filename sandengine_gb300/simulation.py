@@ -127,6 +127,25 @@ class Simulation:
         check(lib().se_world_device_grid(self._h, ctypes.byref(p)))
         return p.value or 0
 
+    def autotune(self, reps: int = 3) -> int:
+        """Pick the fastest tile shape / frames per launch for this world (state unchanged);
+        returns the chosen frames per launch."""
+        k = ctypes.c_int(0)
+        check(lib().se_world_autotune(self._h, int(reps), ctypes.byref(k)))
+        return k.value
+
+    def set_timing(self, enable: bool) -> None:
+        """Bracket every tile-kernel launch with CUDA events (see read_timing)."""
+        check(lib().se_world_set_timing(self._h, 1 if enable else 0))
+
+    def read_timing(self) -> dict:
+        """Kernel time, launches, cell updates and cells read by tile launches since the
+        last read (synchronizes)."""
+        ms, n, cf, c = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        check(lib().se_world_read_timing(self._h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(cf),
+                                         ctypes.byref(c)))
+        return {"kernel_ms": ms.value, "launches": n.value, "cell_frames": cf.value, "cells": c.value}
+
     def digest(self) -> int:
         d = ctypes.c_uint64(0)
         check(lib().se_world_digest(self._h, ctypes.byref(d)))

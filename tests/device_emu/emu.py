@@ -2,7 +2,8 @@
 
 Compiles the exact source handed to NVRTC (Ruleset.kernel_source) with g++ against
 cuda_host_shim.hpp and runs the tile kernels with one thread per CTA (see the shim's
-header) and the edit kernel thread by thread.
+header) and the edit kernel thread by thread.  With ``lut=False`` the block transition
+table is compiled out, so the direct rule-evaluation path runs instead.
 """
 import ctypes
 import hashlib
@@ -18,17 +19,28 @@ VARIANTS = [(128, 64, 1), (256, 32, 1), (128, 32, 1), (128, 64, 2), (128, 64, 4)
             (128, 128, 8), (128, 128, 16), (256, 64, 4), (64, 64, 4)]
 
 DRIVER = r'''
-alignas(16) uint8_t se_smem[1 << 20];
+alignas(16) uint8_t se_smem[1 << 21];
+static uint16_t* g_lut = nullptr;
+extern "C" int emu_build_lut() {
+#ifdef SE_LUT
+  g_lut = new uint16_t[SE_LUT_ENTRIES];
+  blockDim.x = 1; gridDim.x = 1; threadIdx.x = 0; blockIdx.x = 0;
+  se_build_lut(g_lut);
+  return 1;
+#else
+  return 0;
+#endif
+}
 #define EMU_TILE(TW, TH, K) \
 extern "C" void emu_tile_##TW##x##TH##_k##K(const uint32_t* src, uint32_t* dst, int W, int H, int f0, int k) { \
   blockDim.x = 1; threadIdx.x = 0; \
   for (unsigned by = 0; by < (unsigned)((H + TH - 1) / TH); ++by) \
     for (unsigned bx = 0; bx < (unsigned)((W + TW - 1) / TW); ++bx) { \
       blockIdx.x = bx; blockIdx.y = by; \
-      se_tile_impl<TW, TH, K, 1>(src, dst, W, H, f0, k); \
+      se_tile_impl<TW, TH, K, 1>(src, dst, W, H, f0, k, g_lut); \
     } \
 }
-%s
+@TILES@
 extern "C" void emu_edit(uint32_t* grid, int W, int H, int nmods, long long total, const void* params) {
   const SeEditParams& p = *reinterpret_cast<const SeEditParams*>(params);
   blockDim.x = 256;
@@ -42,11 +54,15 @@ extern "C" void emu_edit(uint32_t* grid, int W, int H, int nmods, long long tota
 
 
 class Emu:
-    def __init__(self, ruleset):
+    def __init__(self, ruleset, lut: bool = True):
         src = ruleset.kernel_source
+        if not lut:
+            src = src.replace("#define SE_LUT 1\n", "")
         tiles = "\n".join(f"EMU_TILE({a}, {b}, {c})" for a, b, c in VARIANTS)
-        code = '#include "cuda_host_shim.hpp"\n' + src + DRIVER.replace('%s', tiles)
-        key = hashlib.sha256((code + open(os.path.join(HERE, "cuda_host_shim.hpp")).read()).encode()).hexdigest()[:16]
+        code = '#include "cuda_host_shim.hpp"\n' + src + DRIVER.replace("@TILES@", tiles)
+        with open(os.path.join(HERE, "cuda_host_shim.hpp")) as f:
+            shim = f.read()
+        key = hashlib.sha256((code + shim).encode()).hexdigest()[:16]
         d = os.path.join(OUT, "emu_" + key)
         so = os.path.join(d, "emu.so")
         if not os.path.exists(so):
@@ -63,6 +79,7 @@ class Emu:
             os.replace(tmp, so)
         self.lib = ctypes.CDLL(so)
         self.nmat = ruleset.num_materials
+        self.has_lut = bool(self.lib.emu_build_lut())
 
     def tiles(self, src: np.ndarray, f0: int, k: int, variant=None) -> np.ndarray:
         """k frames (counters f0..f0+k-1) with one launch of the tile kernel."""

@@ -104,6 +104,36 @@ def test_edits_inside_fused_runs(se, ports, rulesets):
         assert np.array_equal(sim.grid, g), f"round {r}"
 
 
+POS_RULE = """
+  ledge:
+    if: isType_EMPTY(DOWN) and pos.x + pos.y * 3 - frame % 7 > 11
+    do: SWAP SELF DOWN
+"""
+
+
+def test_direct_path_matches_port(se, rulesets):
+    """A rule that reads the block position and the frame cannot use the block transition
+    table; the direct rule-evaluation path must be exact too."""
+    from oracle.build import Port
+    from sandengine_gb300 import workloads as wl
+    text = rulesets["four_materials"].replace("rules:\n", "rules:\n" + POS_RULE.lstrip("\n"), 1)
+    text = text.replace("base_rules: [fall]", "base_rules: [fall, ledge]")
+    rs = se.parse_string(text)
+    assert "SE_LUT" not in rs.cuda_source
+    port = Port(text)
+    w, h = 203, 131
+    g = wl.iid_fill(w, h, 5, *wl.FOUR_FILL)
+    for k in (1, 4):
+        sim = se.Simulation(rs, (w, h))
+        sim.set_steps_per_launch(k)
+        a = g.copy()
+        sim.grid = a
+        sim.params.frame = 3
+        sim.run_frames(40)
+        port.run(a, 3, 40)
+        assert np.array_equal(sim.grid, a), f"k={k}"
+
+
 def test_frame_one_clears(se, rulesets):
     g = np.full((40, 40), 3, dtype=np.uint32)
     sim = _sim(se, rulesets["four_materials"], 40, 40)

@@ -8,9 +8,10 @@ from sandengine_gb300 import workloads as wl
 from tests.device_emu.emu import VARIANTS, Emu
 
 
-@pytest.fixture(scope="module")
-def emus(se, rulesets):
-    return {n: Emu(se.parse_string(t)) for n, t in rulesets.items()}
+@pytest.fixture(scope="module", params=[True, False], ids=["table", "direct"])
+def emus(se, rulesets, request):
+    """Kernels with the block transition table, and with it compiled out."""
+    return {n: Emu(se.parse_string(t), lut=request.param) for n, t in rulesets.items()}
 
 
 def _world(name, w, h, seed):
