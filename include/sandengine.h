@@ -138,6 +138,24 @@ int se_world_digest(se_world* w, uint64_t* digest);
  * values >= nbins-1.  nbins in [1, 257].  Synchronizes the stream.  (No counterpart in the
  * reference: material-conservation checks.) */
 int se_world_histogram(se_world* w, uint64_t* counts, int nbins);
+/* The same material counts as se_world_histogram, for any grid already on the device
+ * (`count` uint32 cells at `device_cells`), WITHOUT allocating: no cudaMalloc, cudaFree or
+ * allocating library call.  It exists for callers that cannot allocate device memory at
+ * the point they need the counts: a frame loop that sized all of its GPU memory up front
+ * and may not allocate per frame, a serving process whose HBM budget is already fully
+ * committed to resident worlds, or code running while another allocator (e.g. a framework's
+ * caching allocator) holds the free memory.  The counters live in a static device array of
+ * SE_NOALLOC_MAX_BINS (257) 64-bit words, 2,056 bytes, which every GPU that loads the
+ * library keeps until the process exits; nbins above 257 is rejected with
+ * SE_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's device address
+ * (make that first call before any stream capture).  Every call shares the array: it clears
+ * the counters on `cuda_stream` (NULL = the legacy default stream), counts, copies nbins
+ * counters to host_counts and synchronizes the stream before returning, so calls from one
+ * thread never overlap; calls from different threads or streams that overlap on the GPU
+ * race on the counters.  (No counterpart in the reference.) */
+#define SE_NOALLOC_MAX_BINS 257
+int se_grid_histogram_noalloc(const uint32_t* device_cells, uint64_t count, int nbins, uint64_t* host_counts,
+                              void* cuda_stream);
 /* Opt-in timing of the Margolus tile kernel: with enable != 0, every tile launch is
  * bracketed by CUDA events on the world's stream.  se_world_read_timing synchronizes and
  * returns, since the last read, the summed kernel time, the number of launches, the cell

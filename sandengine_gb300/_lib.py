@@ -76,6 +76,7 @@ _SIGS = {
     "se_world_histogram": ([_P, _P, _I], _I),
     "se_world_set_timing": ([_P, _I], _I),
     "se_world_autotune": ([_P, _I, ctypes.POINTER(_I)], _I),
+    "se_grid_histogram_noalloc": ([_P, ctypes.c_uint64, _I, _P, _P], _I),
     "se_world_read_timing": ([_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                               ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)], _I),
 }

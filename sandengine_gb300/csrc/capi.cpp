@@ -277,6 +277,25 @@ SE_API int se_world_histogram(se_world* w, uint64_t* counts, int nbins) {
   });
 }
 
+// Material counts of any device grid without allocating device memory: the counters live
+// in a fixed static device array (see se_grid_histogram_noalloc in include/sandengine.h).
+SE_API int se_grid_histogram_noalloc(const uint32_t* device_cells, uint64_t count, int nbins,
+                                     uint64_t* host_counts, void* cuda_stream) {
+  return guard([&] {
+    if (!device_cells || !host_counts) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    const int maxb = se::rt::noalloc_max_bins();
+    if (nbins < 1 || nbins > maxb)
+      return fail(SE_ERR_INVALID_ARGUMENT, "nbins must be in [1, " + std::to_string(maxb) +
+                                               "]: the allocation-free histogram has a fixed scratch of " +
+                                               std::to_string(maxb) + " counters");
+    cudaError_t e = se::rt::histogram_noalloc(device_cells, (unsigned long long)count, nbins,
+                                              reinterpret_cast<unsigned long long*>(host_counts),
+                                              (cudaStream_t)cuda_stream);
+    if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("histogram (no-alloc): ") + cudaGetErrorString(e));
+    return (int)SE_OK;
+  });
+}
+
 SE_API int se_world_autotune(se_world* w, int reps, int* best_k) {
   return guard([&] {
     if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");

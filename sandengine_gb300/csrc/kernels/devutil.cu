@@ -4,6 +4,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
+// Counters for se_grid_histogram_noalloc, in the module's own static device memory so
+// that entry point never allocates.  257 counters (2,056 bytes); every GPU that loads the
+// library keeps this array until the process exits.  All calls share it.
+#define SE_NOALLOC_MAX_BINS 257
+static __device__ __align__(256) unsigned long long se_noalloc_hist[SE_NOALLOC_MAX_BINS];
+
 namespace {
 
 __device__ __forceinline__ unsigned long long se_mix64(unsigned long long z) {
@@ -71,6 +79,48 @@ cudaError_t grid_histogram(const uint32_t* g, unsigned long long n, int nbins, u
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   se_histogram_kernel<<<sms * 4, 256, 0, s>>>(g, n, nbins, d_counts);
   return cudaGetLastError();
+}
+
+int noalloc_max_bins() { return SE_NOALLOC_MAX_BINS; }
+
+// The histogram of grid_histogram, counted in se_noalloc_hist instead of caller- or
+// library-allocated memory.  The host must not pass the array's name to a kernel (in host
+// code it is a stand-in, not a device address), so the device address is looked up once
+// per device, with that device current, and cached.  The counters are cleared on the
+// stream before each use; the results are copied to host_counts and the stream is
+// synchronized before returning.
+cudaError_t histogram_noalloc(const uint32_t* g, unsigned long long n, int nbins, unsigned long long* host_counts,
+                              cudaStream_t s) {
+  constexpr int kMaxDevices = 64;
+  static unsigned long long* addr[kMaxDevices] = {};
+  static std::mutex mu;
+  if (nbins < 1 || nbins > SE_NOALLOC_MAX_BINS) return cudaErrorInvalidValue;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  unsigned long long* p = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+      void* q = nullptr;
+      e = cudaGetSymbolAddress(&q, se_noalloc_hist);
+      if (e != cudaSuccess) return e;
+      addr[dev] = static_cast<unsigned long long*>(q);
+    }
+    p = addr[dev];
+  }
+  e = cudaMemsetAsync(p, 0, sizeof(unsigned long long) * (size_t)nbins, s);
+  if (e != cudaSuccess) return e;
+  int sms = 0;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  se_histogram_kernel<<<sms * 4, 256, 0, s>>>(g, n, nbins, p);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(host_counts, p, sizeof(unsigned long long) * (size_t)nbins, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(s);
 }
 
 }  // namespace se::rt

@@ -88,5 +88,8 @@ struct World {
 cudaError_t grid_digest(const uint32_t* g, unsigned long long n, unsigned long long* d_out, cudaStream_t s);
 cudaError_t grid_histogram(const uint32_t* g, unsigned long long n, int nbins, unsigned long long* d_counts,
                            cudaStream_t s);
+int noalloc_max_bins();
+cudaError_t histogram_noalloc(const uint32_t* g, unsigned long long n, int nbins, unsigned long long* host_counts,
+                              cudaStream_t s);
 
 }  // namespace se::rt
