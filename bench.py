@@ -83,8 +83,9 @@ def load_peak():
         return 6800.0, "fallback"
 
 
-def load_traffic(k, workload_name):
-    """DRAM bytes per tile-kernel launch from the committed ncu summary, if it covers this k."""
+def load_traffic(cells_per_launch):
+    """DRAM bytes of one tile-kernel launch: the committed ncu capture's bytes per cell (an
+    8192^2 world of the same family) scaled to the launch's cells."""
     p = os.path.join(ROOT, "profiles", "tile_kernel_traffic.txt")
     if not os.path.exists(p):
         return None
@@ -94,11 +95,9 @@ def load_traffic(k, workload_name):
             a, b = line.strip().split("=", 1)
             vals[a.strip()] = b.strip()
     try:
-        if int(vals.get("k", -1)) == k and vals.get("workload") == workload_name:
-            return float(vals["dram_bytes_per_launch"])
+        return float(vals["dram_bytes_per_cell"]) * cells_per_launch
     except Exception:
-        pass
-    return None
+        return None
 
 
 class ClockSampler:
@@ -277,7 +276,7 @@ def run_ours(args, rep):
     alg_bytes_per_launch = 8.0 * timing["cells"] / max(launches, 1)
     avg_launch_s = kernel_ms / max(launches, 1) / 1e3
     achieved = alg_bytes_per_launch / avg_launch_s / 1e9 if launches else None
-    traffic = load_traffic(k, spec["name"])
+    traffic = load_traffic(W * H) if spec["ruleset"] == "twelve_materials" else None
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": rep.world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
