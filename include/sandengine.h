@@ -166,6 +166,36 @@ int se_world_set_timing(se_world* w, int enable);
 int se_world_read_timing(se_world* w, double* kernel_ms, long long* launches, long long* cell_frames,
                          long long* cells);
 
+/* ---- many worlds (no counterpart in the reference, which runs one world) --------------- */
+
+typedef struct se_batch se_batch;
+
+/* n independent worlds of the given sizes, all EMPTY, frame 0, in one device arena.
+ * Worlds whose grid (plus a WALL border) fits in one CTA's shared memory are advanced a
+ * whole launch at a time on chip; the others by temporally blocked tile passes. */
+int se_batch_create(se_ruleset* rs, int n, const int* widths, const int* heights, se_batch** out);
+void se_batch_destroy(se_batch* b);
+int se_batch_set_grid(se_batch* b, int world, const uint32_t* cells, size_t count);
+int se_batch_get_grid(se_batch* b, int world, uint32_t* cells, size_t count);
+int se_batch_set_frame(se_batch* b, int world, int32_t frame);
+int se_batch_get_frame(const se_batch* b, int world, int32_t* frame);
+/* Advances every world by nframes frames with one CUDA graph launch (captured on first use
+ * for each nframes): the resident worlds and the tile passes run as concurrent branches
+ * and the frame counters advance on the device.  Either all worlds or none may be at
+ * frame 0 (whose next frame clears, falling_sand.glsl:128-131).  Asynchronous. */
+int se_batch_step(se_batch* b, int nframes);
+/* The same frames with one kernel launch per world per frame, as the reference dispatches
+ * (the baseline the batched launch is measured against). */
+int se_batch_step_plain(se_batch* b, int nframes);
+/* Times every tile shape / fusion depth on the tiled worlds (state unchanged) and keeps
+ * the fastest; *best_k = frames per tile pass. */
+int se_batch_autotune(se_batch* b, int reps, int* best_k);
+int se_batch_set_steps_per_launch(se_batch* b, int k);
+int se_batch_synchronize(se_batch* b);
+int se_batch_get_stream(se_batch* b, void** cuda_stream);
+int se_batch_info(const se_batch* b, int* resident_worlds, int* tiled_worlds, long long* cells,
+                  int* steps_per_launch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,20 @@ _SIGS = {
     "se_world_set_timing": ([_P, _I], _I),
     "se_world_autotune": ([_P, _I, ctypes.POINTER(_I)], _I),
     "se_grid_histogram_noalloc": ([_P, ctypes.c_uint64, _I, _P, _P], _I),
+    "se_batch_create": ([_P, _I, _P, _P, ctypes.POINTER(_P)], _I),
+    "se_batch_destroy": ([_P], None),
+    "se_batch_set_grid": ([_P, _I, _P, ctypes.c_size_t], _I),
+    "se_batch_get_grid": ([_P, _I, _P, ctypes.c_size_t], _I),
+    "se_batch_set_frame": ([_P, _I, ctypes.c_int32], _I),
+    "se_batch_get_frame": ([_P, _I, ctypes.POINTER(ctypes.c_int32)], _I),
+    "se_batch_step": ([_P, _I], _I),
+    "se_batch_step_plain": ([_P, _I], _I),
+    "se_batch_autotune": ([_P, _I, ctypes.POINTER(_I)], _I),
+    "se_batch_set_steps_per_launch": ([_P, _I], _I),
+    "se_batch_synchronize": ([_P], _I),
+    "se_batch_get_stream": ([_P, ctypes.POINTER(_P)], _I),
+    "se_batch_info": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_longlong),
+                       ctypes.POINTER(_I)], _I),
     "se_world_read_timing": ([_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                               ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)], _I),
 }

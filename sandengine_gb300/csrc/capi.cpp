@@ -10,6 +10,7 @@
 #include "../../include/sandengine.h"
 #include "lang/codegen.hpp"
 #include "lang/lang.hpp"
+#include "runtime/batch.hpp"
 #include "runtime/engine.hpp"
 
 #define SE_API extern "C" __attribute__((visibility("default")))
@@ -322,5 +323,120 @@ SE_API int se_world_read_timing(se_world* w, double* kernel_ms, long long* launc
   return guard([&] {
     if (!w || !kernel_ms || !launches || !cell_frames || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
     return ret(w->w->timing_read(kernel_ms, launches, cell_frames, cells));
+  });
+}
+
+// ---- batches ---------------------------------------------------------------------------
+struct se_batch {
+  std::unique_ptr<se::rt::Batch> b;
+};
+
+SE_API int se_batch_create(se_ruleset* rs, int n, const int* widths, const int* heights, se_batch** out) {
+  return guard([&] {
+    if (!rs || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    auto b = std::make_unique<se::rt::Batch>();
+    se::rt::Status s = b->create(rs->rs, n, widths, heights);
+    if (!s.ok()) return ret(s);
+    *out = new se_batch{std::move(b)};
+    return (int)SE_OK;
+  });
+}
+
+SE_API void se_batch_destroy(se_batch* b) {
+  if (b && b->b && b->b->stream) cudaStreamSynchronize(b->b->stream);
+  delete b;
+}
+
+SE_API int se_batch_set_grid(se_batch* b, int world, const uint32_t* cells, size_t count) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    return ret(b->b->set_grid(world, cells, count));
+  });
+}
+
+SE_API int se_batch_get_grid(se_batch* b, int world, uint32_t* cells, size_t count) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    return ret(b->b->get_grid(world, cells, count));
+  });
+}
+
+SE_API int se_batch_set_frame(se_batch* b, int world, int32_t frame) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    return ret(b->b->set_frame(world, frame));
+  });
+}
+
+SE_API int se_batch_get_frame(const se_batch* b, int world, int32_t* frame) {
+  return guard([&] {
+    if (!b || !frame || world < 0 || world >= b->b->n) return fail(SE_ERR_INVALID_ARGUMENT, "bad argument");
+    *frame = b->b->desc[(size_t)world].frame;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_batch_step(se_batch* b, int nframes) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    return ret(b->b->step(nframes));
+  });
+}
+
+SE_API int se_batch_step_plain(se_batch* b, int nframes) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    return ret(b->b->step_plain(nframes));
+  });
+}
+
+SE_API int se_batch_autotune(se_batch* b, int reps, int* best_k) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    return ret(b->b->autotune(reps, best_k));
+  });
+}
+
+SE_API int se_batch_set_steps_per_launch(se_batch* b, int k) {
+  return guard([&] {
+    if (!b || k < 1) return fail(SE_ERR_INVALID_ARGUMENT, "k must be >= 1");
+    const se::rt::TileVariant* v = nullptr;
+    for (auto& t : se::rt::tile_variants())
+      if (t.kmax >= k && (!v || t.kmax < v->kmax)) v = &t;
+    if (!v) return fail(SE_ERR_INVALID_ARGUMENT, "no kernel variant for this many frames per launch");
+    b->b->steps_per_launch = k;
+    return ret(b->b->set_variant(v));
+  });
+}
+
+SE_API int se_batch_synchronize(se_batch* b) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    cudaError_t e = cudaStreamSynchronize(b->b->stream);
+    if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_batch_get_stream(se_batch* b, void** s) {
+  return guard([&] {
+    if (!b || !s) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *s = (void*)b->b->stream;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_batch_info(const se_batch* b, int* resident_worlds, int* tiled_worlds, long long* cells,
+                         int* steps_per_launch) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    int r = 0;
+    for (auto& c : b->b->resident) r += (int)c.ids.size();
+    if (resident_worlds) *resident_worlds = r;
+    if (tiled_worlds) *tiled_worlds = (int)b->b->tiled.size();
+    if (cells) *cells = b->b->cells;
+    if (steps_per_launch) *steps_per_launch = b->b->variant ? b->b->variant->kmax : 0;
+    return (int)SE_OK;
   });
 }

@@ -86,6 +86,46 @@ extern "C" __global__ void __launch_bounds__(256) se_build_lut(uint16_t* __restr
 #define SE_LUT_SMEM_MAX_ENTRIES 16384u
 #endif
 
+// One block's update: the block transition table when the rule set has one, else the
+// generated rules.
+__device__ __forceinline__ void se_block_update(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d, int gx, int gy,
+                                                int f, int W, int H, const uint16_t* __restrict__ lut) {
+#ifdef SE_LUT
+  const uint32_t x = (uint32_t)gx * 461u + (uint32_t)gy * 2131u + (uint32_t)f * 4541161u;
+  const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u), h3 = se_mix(x * 213132u);
+  const uint32_t idx = se_gen::lut_index(a, b, c, d, h0, h1, h2, h3);
+#if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
+  const uint32_t o = lut[idx];  // shared-memory copy
+#else
+  const uint32_t o = __ldg(lut + idx);
+#endif
+  a = o & 15u;
+  b = (o >> 4) & 15u;
+  c = (o >> 8) & 15u;
+  d = o >> 12;
+#else
+  se_block(a, b, c, d, gx, gy, f, W, H);
+#endif
+}
+
+// Writes a block back into the shared array; slots outside the world stay WALL.
+__device__ __forceinline__ void se_block_store(uint8_t* p, int SW, uint32_t a, uint32_t b, uint32_t c, uint32_t d,
+                                               int gx, int gy, int W, int H, bool edge) {
+  if (!edge) {
+    p[0] = (uint8_t)a;
+    p[1] = (uint8_t)b;
+    p[SW] = (uint8_t)c;
+    p[SW + 1] = (uint8_t)d;
+  } else {
+    const bool x0 = gx >= 0 && gx < W, x1 = gx + 1 >= 0 && gx + 1 < W;
+    const bool y0 = gy >= 0 && gy < H, y1 = gy + 1 >= 0 && gy + 1 < H;
+    if (x0 && y0) p[0] = (uint8_t)a;
+    if (x1 && y0) p[1] = (uint8_t)b;
+    if (x0 && y1) p[SW] = (uint8_t)c;
+    if (x1 && y1) p[SW + 1] = (uint8_t)d;
+  }
+}
+
 // One step over the shared array: every block wholly inside it.  OX and ly0 are the
 // parities of the first block column / row in shared-array coordinates: a block's global
 // top-left cell is congruent to the frame's offset modulo 2, and the array starts at global
@@ -102,61 +142,131 @@ __device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int 
     uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
     if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
     const int gx = gx0 + lx, gy = gy0 + ly;
-#ifdef SE_LUT
-    {
-      const uint32_t x = (uint32_t)gx * 461u + (uint32_t)gy * 2131u + (uint32_t)f * 4541161u;
-      const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u),
-                     h3 = se_mix(x * 213132u);
-      const uint32_t idx = se_gen::lut_index(a, b, c, d, h0, h1, h2, h3);
-#if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
-      const uint32_t o = lut[idx];  // shared-memory copy
-#else
-      const uint32_t o = __ldg(lut + idx);
-#endif
-      a = o & 15u;
-      b = (o >> 4) & 15u;
-      c = (o >> 8) & 15u;
-      d = o >> 12;
+    se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
+    se_block_store(p, SW, a, b, c, d, gx, gy, W, H, edge);
+  }
+}
+
+// The same over a shared array whose size is only known at run time (whole worlds); the
+// block index is split with a float reciprocal and a +-1 correction.
+__device__ __forceinline__ void se_step_rt(uint8_t* sm, int SW, int SH, int ox, int ly0, int gx0, int gy0, int f,
+                                           int W, int H, const uint16_t* __restrict__ lut) {
+  const int nbx = (SW - ox) / 2;
+  const int nb = nbx * ((SH - ly0) / 2);
+  const float inv = 1.0f / (float)nbx;
+  for (int bi = threadIdx.x; bi < nb; bi += blockDim.x) {
+    int j = __float2int_rz((float)bi * inv);
+    int i = bi - j * nbx;
+    if (i >= nbx) {
+      ++j;
+      i -= nbx;
+    } else if (i < 0) {
+      --j;
+      i += nbx;
     }
+    const int lx = ox + 2 * i, ly = ly0 + 2 * j;
+    uint8_t* p = sm + ly * SW + lx;
+    uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+    if ((a | b | c | d) == 0u) continue;
+    const int gx = gx0 + lx, gy = gy0 + ly;
+    se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
+    se_block_store(p, SW, a, b, c, d, gx, gy, W, H, true);
+  }
+}
+
+// Copies a small block transition table into shared memory at byte offset `off`;
+// returns the table to use.
+__device__ __forceinline__ const uint16_t* se_lut_to_smem(const uint16_t* __restrict__ lut, uint8_t* smem, int off,
+                                                         int nt) {
+#if defined(SE_LUT) && SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
+  uint16_t* slut = reinterpret_cast<uint16_t*>(smem + off);
+  for (uint32_t i = threadIdx.x; i < SE_LUT_ENTRIES / 2u; i += nt)
+    reinterpret_cast<uint32_t*>(slut)[i] = __ldg(reinterpret_cast<const uint32_t*>(lut) + i);
+  return slut;
 #else
-    se_block(a, b, c, d, gx, gy, f, W, H);
+  return lut;
 #endif
-    if (!edge) {
-      p[0] = (uint8_t)a;
-      p[1] = (uint8_t)b;
-      p[SW] = (uint8_t)c;
-      p[SW + 1] = (uint8_t)d;
+}
+
+// Loads rows [gy0, gy0 + SH) x columns [gx0, gx0 + SW) of a W x H grid into the u8 array
+// (row stride SW, a multiple of 4; gx0 a multiple of 4): ids normalised, outside = WALL.
+__device__ __forceinline__ void se_load_region(uint8_t* sm, int SW, int SH, const uint32_t* __restrict__ src, int W,
+                                               int H, int gx0, int gy0, int nt) {
+  const int wpr = SW / 4;
+  const bool vec = (W & 3) == 0;
+  const float inv = 1.0f / (float)wpr;
+  for (int i = threadIdx.x; i < wpr * SH; i += nt) {
+    int r = __float2int_rz((float)i * inv);
+    int c = i - r * wpr;
+    if (c >= wpr) {
+      ++r;
+      c -= wpr;
+    } else if (c < 0) {
+      --r;
+      c += wpr;
+    }
+    const int gy = gy0 + r, gx = gx0 + 4 * c;
+    uint32_t packed;
+    if (gy < 0 || gy >= H) {
+      packed = 0x02020202u;
+    } else if (vec && gx >= 0 && gx + 3 < W) {
+      const uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (size_t)gy * W + gx));
+      packed = se_norm(v.x) | (se_norm(v.y) << 8) | (se_norm(v.z) << 16) | (se_norm(v.w) << 24);
     } else {
-      const bool x0 = gx >= 0 && gx < W, x1 = gx + 1 >= 0 && gx + 1 < W;
-      const bool y0 = gy >= 0 && gy < H, y1 = gy + 1 >= 0 && gy + 1 < H;
-      if (x0 && y0) p[0] = (uint8_t)a;
-      if (x1 && y0) p[1] = (uint8_t)b;
-      if (x0 && y1) p[SW] = (uint8_t)c;
-      if (x1 && y1) p[SW + 1] = (uint8_t)d;
+      packed = 0;
+      for (int e = 0; e < 4; ++e) {
+        const int x = gx + e;
+        const uint32_t id = (x >= 0 && x < W) ? se_norm(__ldg(src + (size_t)gy * W + x)) : SE_WALL;
+        packed |= id << (8 * e);
+      }
+    }
+    *reinterpret_cast<uint32_t*>(sm + r * SW + 4 * c) = packed;
+  }
+}
+
+// Stores the rows [0, TH) x columns [0, TW) of the array region that starts at (hx, hy)
+// to the grid at (X0, Y0), clipped to the world.
+__device__ __forceinline__ void se_store_region(const uint8_t* sm, int SW, int hx, int hy, int TW, int TH,
+                                                uint32_t* __restrict__ dst, int W, int H, int X0, int Y0, int nt) {
+  const int owpr = (TW + 3) / 4;
+  const bool vec = (W & 3) == 0;
+  const float inv = 1.0f / (float)owpr;
+  for (int i = threadIdx.x; i < owpr * TH; i += nt) {
+    int r = __float2int_rz((float)i * inv);
+    int c = i - r * owpr;
+    if (c >= owpr) {
+      ++r;
+      c -= owpr;
+    } else if (c < 0) {
+      --r;
+      c += owpr;
+    }
+    const int gy = Y0 + r, gx = X0 + 4 * c;
+    if (gy >= H || gx >= W) continue;
+    const uint32_t packed = *reinterpret_cast<const uint32_t*>(sm + (r + hy) * SW + hx + 4 * c);
+    if (vec && gx + 3 < W) {
+      const uint4 v = make_uint4(packed & 0xffu, (packed >> 8) & 0xffu, (packed >> 16) & 0xffu, packed >> 24);
+      *reinterpret_cast<uint4*>(dst + (size_t)gy * W + gx) = v;
+    } else {
+      for (int e = 0; e < 4; ++e)
+        if (gx + e < W) dst[(size_t)gy * W + gx + e] = (packed >> (8 * e)) & 0xffu;
     }
   }
 }
 
-// Advances the tile (blockIdx.x, blockIdx.y) of a W x H world by k <= KMAX frames whose
+// Advances the tile with top-left cell (X0, Y0) of a W x H world by k <= KMAX frames whose
 // counters are f0, f0+1, ... (all >= 2; the host handles the frame-1 clear).
 template <int TW, int TH, int KMAX, int NT>
-__device__ __forceinline__ void se_tile_impl(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W,
-                                             int H, int f0, int k, const uint16_t* __restrict__ lut) {
+__device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W,
+                                            int H, int f0, int k, const uint16_t* __restrict__ lut, int X0, int Y0) {
   constexpr int HX = ((KMAX + 3) / 4) * 4, HY = KMAX;
   constexpr int SW = TW + 2 * HX, SH = TH + 2 * HY, WPR = SW / 4;
   static_assert(TW % 4 == 0, "tile width must be a multiple of 4");
+  static_assert(HX % 2 == 0 && TW % 2 == 0, "gx0 must be even");
   extern __shared__ __align__(16) uint8_t se_smem[];
   uint8_t* sm = se_smem;
   se_gen::init_tables(threadIdx.x, NT);
-#if defined(SE_LUT) && SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
-  {  // small tables live in shared memory, after the tile
-    uint16_t* slut = reinterpret_cast<uint16_t*>(se_smem + ((SW * SH + 15) & ~15));
-    for (uint32_t i = threadIdx.x; i < SE_LUT_ENTRIES / 2u; i += NT)
-      reinterpret_cast<uint32_t*>(slut)[i] = __ldg(reinterpret_cast<const uint32_t*>(lut) + i);
-    lut = slut;
-  }
-#endif
-  const int X0 = blockIdx.x * TW, Y0 = blockIdx.y * TH;
+  lut = se_lut_to_smem(lut, se_smem, (SW * SH + 15) & ~15, NT);
   const int gx0 = X0 - HX, gy0 = Y0 - HY;
   const bool vec = (W & 3) == 0;
 
@@ -182,7 +292,6 @@ __device__ __forceinline__ void se_tile_impl(const uint32_t* __restrict__ src, u
   __syncthreads();
 
   const bool edge = gx0 < 0 || gy0 < 0 || gx0 + SW > W || gy0 + SH > H;
-  static_assert(HX % 2 == 0 && TW % 2 == 0, "gx0 must be even");
   for (int s = 0; s < k; ++s) {
     const int f = f0 + s;
     const int ly0 = (se_off_y(f) + gy0) & 1;  // gy0 = Y0 - HY is odd when HY is
@@ -206,6 +315,80 @@ __device__ __forceinline__ void se_tile_impl(const uint32_t* __restrict__ src, u
       for (int e = 0; e < 4; ++e)
         if (gx + e < W) dst[(size_t)gy * W + gx + e] = (packed >> (8 * e)) & 0xffu;
     }
+  }
+}
+
+// Single world: the tile is (blockIdx.x, blockIdx.y).
+template <int TW, int TH, int KMAX, int NT>
+__device__ __forceinline__ void se_tile_impl(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W,
+                                             int H, int f0, int k, const uint16_t* __restrict__ lut) {
+  se_tile_run<TW, TH, KMAX, NT>(src, dst, W, H, f0, k, lut, blockIdx.x * TW, blockIdx.y * TH);
+}
+
+// ---- many worlds -------------------------------------------------------------------------
+// A world of a batch.  `frame` is the counter before its next frame and `cur` the buffer
+// holding its grid; both live on the device and advance in se_batch_finalize, so repeated
+// launches of a captured graph need no host updates.
+struct SeWorldDesc {
+  uint32_t* buf0;
+  uint32_t* buf1;
+  int W, H;
+  int frame;
+  int cur;
+  int pad0, pad1;
+};
+// One tile job: a tile of a world too large to stay in shared memory.
+struct SeTileJob {
+  int world, x0, y0, pad;
+};
+
+// Pass `pass` of a multi-pass launch: k frames for every tile job, after `frames_done`
+// frames of earlier passes.  The grid to read is the world's buffer cur ^ (pass & 1).
+template <int TW, int TH, int KMAX, int NT>
+__device__ __forceinline__ void se_mtile_impl(const SeWorldDesc* __restrict__ worlds,
+                                              const SeTileJob* __restrict__ jobs, int pass, int frames_done, int k,
+                                              const uint16_t* __restrict__ lut) {
+  const SeTileJob job = jobs[blockIdx.x];
+  const SeWorldDesc w = worlds[job.world];
+  const int in = w.cur ^ (pass & 1);
+  const uint32_t* src = in ? w.buf1 : w.buf0;
+  uint32_t* dst = in ? w.buf0 : w.buf1;
+  se_tile_run<TW, TH, KMAX, NT>(src, dst, w.W, w.H, w.frame + 1 + frames_done, k, lut, job.x0, job.y0);
+}
+
+// Whole-world launch: CTA b holds world ids[b] entirely in shared memory (plus a WALL
+// border: 4 columns each side for aligned loads, 1 row above and below), advances it by
+// `frames` frames and stores it to the buffer cur ^ out_flip.  Nothing outside the world is
+// ever written back, so the border stays WALL for every frame, as getCell returns there.
+extern "C" __global__ void __launch_bounds__(1024) se_resident(const SeWorldDesc* __restrict__ worlds,
+                                                               const int* __restrict__ ids, int frames, int out_flip,
+                                                               const uint16_t* __restrict__ lut) {
+  extern __shared__ __align__(16) uint8_t se_smem[];
+  const SeWorldDesc w = worlds[ids[blockIdx.x]];
+  const int SW = ((w.W + 3) & ~3) + 8, SH = w.H + 2;
+  const int gx0 = -4, gy0 = -1;
+  se_gen::init_tables(threadIdx.x, blockDim.x);
+  lut = se_lut_to_smem(lut, se_smem, (SW * SH + 15) & ~15, blockDim.x);
+  const uint32_t* src = w.cur ? w.buf1 : w.buf0;
+  uint32_t* dst = (w.cur ^ out_flip) ? w.buf1 : w.buf0;
+  se_load_region(se_smem, SW, SH, src, w.W, w.H, gx0, gy0, blockDim.x);
+  __syncthreads();
+  for (int s = 0; s < frames; ++s) {
+    const int f = w.frame + 1 + s;
+    se_step_rt(se_smem, SW, SH, se_off_x(f), (se_off_y(f) + gy0) & 1, gx0, gy0, f, w.W, w.H, lut);
+    __syncthreads();
+  }
+  se_store_region(se_smem, SW, 4, 1, w.W, w.H, dst, w.W, w.H, 0, 0, blockDim.x);
+}
+
+// After a launch of `frames` frames in `passes` passes: advance every world's counter and
+// current buffer.
+extern "C" __global__ void __launch_bounds__(256) se_batch_finalize(SeWorldDesc* __restrict__ worlds, int n,
+                                                                    int frames, int passes) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    worlds[i].frame += frames;
+    worlds[i].cur ^= passes & 1;
   }
 }
 

@@ -39,8 +39,17 @@ std::string kernel_source(const std::string& generated_rules) {
          " const uint16_t* __restrict__ lut) {\n"
       << "  se_tile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
       << ">(src, dst, W, H, f0, k, lut);\n}\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(" << t.nt << ") " << t.multi_name()
+      << "(const SeWorldDesc* __restrict__ worlds, const SeTileJob* __restrict__ jobs, int pass,"
+         " int frames_done, int k, const uint16_t* __restrict__ lut) {\n"
+      << "  se_mtile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
+      << ">(worlds, jobs, pass, frames_done, k, lut);\n}\n";
   }
   return o.str();
+}
+
+std::string TileVariant::multi_name() const {
+  return "se_mtile_" + std::to_string(tw) + "x" + std::to_string(th) + "_k" + std::to_string(kmax);
 }
 
 namespace {
@@ -150,9 +159,12 @@ bool Module::load(const std::string& cubin, unsigned long long lut_entries, std:
     lib = nullptr;
     return false;
   }
-  std::vector<std::string> names = {"se_edit"};
+  std::vector<std::string> names = {"se_edit", "se_resident", "se_batch_finalize"};
   if (lut_entries) names.push_back("se_build_lut");
-  for (auto& t : tile_variants()) names.push_back(t.name());
+  for (auto& t : tile_variants()) {
+    names.push_back(t.name());
+    names.push_back(t.multi_name());
+  }
   for (auto& n : names) {
     cudaKernel_t k;
     e = cudaLibraryGetKernel(&k, lib, n.c_str());
@@ -163,12 +175,31 @@ bool Module::load(const std::string& cubin, unsigned long long lut_entries, std:
     kernels[n] = k;
   }
   for (auto& t : tile_variants()) {
-    e = cudaFuncSetAttribute((const void*)kernels[t.name()], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tile_smem_bytes(t, lut_entries));
-    if (e != cudaSuccess) {
-      *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
-      return false;
+    for (const std::string& n : {t.name(), t.multi_name()}) {
+      e = cudaFuncSetAttribute((const void*)kernels[n], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)tile_smem_bytes(t, lut_entries));
+      if (e != cudaSuccess) {
+        *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+        return false;
+      }
     }
+  }
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  e = cudaFuncGetAttributes(&fa, (const void*)kernels["se_resident"]);
+  if (e != cudaSuccess) {
+    *err = std::string("cudaFuncGetAttributes(se_resident): ") + cudaGetErrorString(e);
+    return false;
+  }
+  // static shared memory (the rule set's property tables) counts against the same limit
+  max_dyn_smem = (size_t)optin - fa.sharedSizeBytes;
+  e = cudaFuncSetAttribute((const void*)kernels["se_resident"], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)max_dyn_smem);
+  if (e != cudaSuccess) {
+    *err = std::string("cudaFuncSetAttribute(se_resident): ") + cudaGetErrorString(e);
+    return false;
   }
   return true;
 }

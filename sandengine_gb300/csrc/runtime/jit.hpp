@@ -13,7 +13,8 @@ namespace se::rt {
 // A tile-kernel instantiation: TW x TH output cells, up to KMAX frames per launch.
 struct TileVariant {
   int tw, th, kmax, nt;
-  std::string name() const;
+  std::string name() const;        // single-world kernel
+  std::string multi_name() const;  // many-world (tile job list) kernel
   int halo_x() const { return ((kmax + 3) / 4) * 4; }
   int halo_y() const { return kmax; }
   size_t smem_bytes() const { return (size_t)(tw + 2 * halo_x()) * (size_t)(th + 2 * halo_y()); }
@@ -36,6 +37,7 @@ bool compile_cubin(const std::string& src, std::string* cubin, std::string* log)
 struct Module {
   cudaLibrary_t lib = nullptr;
   std::map<std::string, cudaKernel_t> kernels;
+  size_t max_dyn_smem = 0;  // opt-in dynamic shared memory per CTA on this device
   ~Module();
   bool load(const std::string& cubin, unsigned long long lut_entries, std::string* err);
   cudaKernel_t get(const std::string& name) const;

@@ -41,6 +41,30 @@ extern "C" void emu_tile_##TW##x##TH##_k##K(const uint32_t* src, uint32_t* dst, 
     } \
 }
 @TILES@
+#define EMU_MTILE(TW, TH, K) \
+extern "C" void emu_mtile_##TW##x##TH##_k##K(const SeWorldDesc* worlds, const SeTileJob* jobs, int njobs, \
+                                             int pass, int done, int k) { \
+  blockDim.x = 1; threadIdx.x = 0; \
+  for (int j = 0; j < njobs; ++j) { \
+    blockIdx.x = j; \
+    se_mtile_impl<TW, TH, K, 1>(worlds, jobs, pass, done, k, g_lut); \
+  } \
+}
+@MTILES@
+extern "C" void emu_resident(const SeWorldDesc* worlds, const int* ids, int nids, int frames, int flip) {
+  blockDim.x = 1; threadIdx.x = 0;
+  for (int j = 0; j < nids; ++j) {
+    blockIdx.x = j;
+    se_resident(worlds, ids, frames, flip, g_lut);
+  }
+}
+extern "C" void emu_finalize(SeWorldDesc* worlds, int n, int frames, int passes) {
+  blockDim.x = 1; threadIdx.x = 0;
+  for (int i = 0; i < n; ++i) {
+    blockIdx.x = i;
+    se_batch_finalize(worlds, n, frames, passes);
+  }
+}
 extern "C" void emu_edit(uint32_t* grid, int W, int H, int nmods, long long total, const void* params) {
   const SeEditParams& p = *reinterpret_cast<const SeEditParams*>(params);
   blockDim.x = 256;
@@ -59,7 +83,9 @@ class Emu:
         if not lut:
             src = src.replace("#define SE_LUT 1\n", "")
         tiles = "\n".join(f"EMU_TILE({a}, {b}, {c})" for a, b, c in VARIANTS)
-        code = '#include "cuda_host_shim.hpp"\n' + src + DRIVER.replace("@TILES@", tiles)
+        mtiles = "\n".join(f"EMU_MTILE({a}, {b}, {c})" for a, b, c in VARIANTS)
+        code = ('#include "cuda_host_shim.hpp"\n' + src +
+                DRIVER.replace("@TILES@", tiles).replace("@MTILES@", mtiles))
         with open(os.path.join(HERE, "cuda_host_shim.hpp")) as f:
             shim = f.read()
         key = hashlib.sha256((code + shim).encode()).hexdigest()[:16]
@@ -91,6 +117,38 @@ class Emu:
         dst = np.zeros_like(src)
         fn(src.ctypes.data, dst.ctypes.data, W, H, f0, k)
         return dst
+
+    def batch(self, grids, frames0, F, k, resident, variant=(128, 64, 8)):
+        """Advances worlds by F frames the way a batch launch does: worlds in ``resident``
+        by the whole-world kernel, the others by ceil(F/k) tile passes, then finalize.
+        Returns the new grids and frame counters."""
+        n = len(grids)
+        desc = np.zeros(n, dtype=[("b0", "<u8"), ("b1", "<u8"), ("W", "<i4"), ("H", "<i4"), ("frame", "<i4"),
+                                  ("cur", "<i4"), ("p0", "<i4"), ("p1", "<i4")])
+        bufs = []
+        for i, g in enumerate(grids):
+            a, b = np.ascontiguousarray(g, dtype=np.uint32).copy(), np.zeros_like(g, dtype=np.uint32)
+            bufs.append((a, b))
+            desc[i] = (a.ctypes.data, b.ctypes.data, g.shape[1], g.shape[0], frames0[i], 0, 0, 0)
+        tiled = [i for i in range(n) if i not in resident]
+        P = (F + k - 1) // k if tiled else 0
+        vp = ctypes.c_void_p
+        if resident:
+            ids = np.array(resident, dtype=np.int32)
+            self.lib.emu_resident.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+            self.lib.emu_resident(desc.ctypes.data, ids.ctypes.data, len(ids), F, P & 1)
+        if tiled:
+            tw, th, _ = variant
+            jobs = np.array([(w, x, y, 0) for w in tiled for y in range(0, grids[w].shape[0], th)
+                             for x in range(0, grids[w].shape[1], tw)], dtype=np.int32)
+            fn = getattr(self.lib, "emu_mtile_%dx%d_k%d" % variant)
+            fn.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+            for p in range(P):
+                fn(desc.ctypes.data, jobs.ctypes.data, len(jobs), p, p * k, min(k, F - p * k))
+        self.lib.emu_finalize.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        self.lib.emu_finalize(desc.ctypes.data, n, F, P)
+        out = [bufs[i][int(desc[i]["cur"])] for i in range(n)]
+        return out, [int(f) for f in desc["frame"]]
 
     def edit(self, grid: np.ndarray, mods) -> None:
         """The edit pass in place; host-side preparation as in runtime/engine.cpp."""

@@ -42,6 +42,22 @@ def test_tile_variants_match_port(emus, ports, name, shape):
             a = b
 
 
+@pytest.mark.parametrize("name", ["four_materials", "twelve_materials"])
+def test_batch_kernels_match_port(emus, ports, name):
+    """Whole-world (resident) kernel, multi-world tile passes and the finalize step."""
+    E, P = emus[name], ports[name]
+    sizes = [(64, 64), (96, 160), (33, 17), (128, 70), (260, 130), (7, 9)]
+    grids = [_world(name, w, h, 10 + i) for i, (w, h) in enumerate(sizes)]
+    frames0 = [1 + 3 * i for i in range(len(sizes))]
+    for F, k, resident in ((13, 8, [0, 2, 4]), (9, 4, []), (6, 16, list(range(6)))):
+        out, fr = E.batch(grids, frames0, F, k, resident, variant=(128, 64, 8) if k <= 8 else (128, 128, 16))
+        for i, g in enumerate(grids):
+            want = g.copy()
+            P.run(want, frames0[i], F)
+            assert np.array_equal(out[i], want), f"world {i} ({sizes[i]}) F={F} k={k} resident={i in resident}"
+            assert fr[i] == frames0[i] + F
+
+
 @pytest.mark.parametrize("name", ["reference", "twelve_materials"])
 def test_edit_pass_matches_port(emus, ports, name):
     w, h = 300, 200
