@@ -196,6 +196,46 @@ int se_batch_get_stream(se_batch* b, void** cuda_stream);
 int se_batch_info(const se_batch* b, int* resident_worlds, int* tiled_worlds, long long* cells,
                   int* steps_per_launch);
 
+/* ---- serving (no counterpart in the reference) ---------------------------------------- */
+
+typedef struct se_server se_server;
+
+typedef struct se_server_stats {
+  long long requests;          /* requests served by the last run */
+  double p50_ms, p99_ms;       /* latency percentiles: completion on the GPU minus arrival */
+  double mean_ms, max_ms;
+  double wall_ms;              /* run start to the last completion */
+  double cell_updates;         /* cells x frames advanced by the last run */
+  long long iterations;        /* batched iterations (plain path: requests) */
+  long long evictions, restores;
+  long long peak_resident_bytes;
+} se_server_stats;
+
+/* A server whose sessions' grids (two u32 buffers each) share one HBM arena of
+ * budget_bytes; sessions that do not fit are evicted to host memory, least recently used
+ * first, and restored when a request needs them. */
+int se_server_create(se_ruleset* rs, long long budget_bytes, se_server** out);
+void se_server_destroy(se_server* s);
+/* Frames a session may advance per batched iteration (a compiled fusion depth). */
+int se_server_set_frames_per_iteration(se_server* s, int k);
+/* A session with an initial grid (NULL = all EMPTY) and frame counter. */
+int se_server_open_session(se_server* s, int width, int height, const uint32_t* cells, int32_t frame,
+                           int* session);
+int se_server_close_session(se_server* s, int session);
+/* Queues "advance nframes frames, applying mods to the first" for a session, arriving
+ * arrival_ms after the start of the next run.  Requests of one session run in order. */
+int se_server_submit(se_server* s, int session, int nframes, const se_modification* mods, int nmods,
+                     double arrival_ms, int* request);
+/* Serves every queued request in real time: requests are admitted when their arrival time
+ * has passed and memory allows.  plain = 0: continuous batching (every active session
+ * advances in one launch per iteration; sessions join and leave between iterations);
+ * plain = 1: one request at a time, one launch per frame (the reference's dispatch). */
+int se_server_run(se_server* s, int plain);
+int se_server_stats_get(se_server* s, se_server_stats* out);
+int se_server_request_latency(se_server* s, int request, double* latency_ms);
+int se_server_get_grid(se_server* s, int session, uint32_t* cells, size_t count);
+int se_server_get_frame(se_server* s, int session, int32_t* frame);
+
 #ifdef __cplusplus
 }
 #endif

@@ -91,6 +91,17 @@ _SIGS = {
     "se_batch_get_stream": ([_P, ctypes.POINTER(_P)], _I),
     "se_batch_info": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_longlong),
                        ctypes.POINTER(_I)], _I),
+    "se_server_create": ([_P, ctypes.c_longlong, ctypes.POINTER(_P)], _I),
+    "se_server_destroy": ([_P], None),
+    "se_server_set_frames_per_iteration": ([_P, _I], _I),
+    "se_server_open_session": ([_P, _I, _I, _P, ctypes.c_int32, ctypes.POINTER(_I)], _I),
+    "se_server_close_session": ([_P, _I], _I),
+    "se_server_submit": ([_P, _I, _I, _P, _I, ctypes.c_double, ctypes.POINTER(_I)], _I),
+    "se_server_run": ([_P, _I], _I),
+    "se_server_stats_get": ([_P, _P], _I),
+    "se_server_request_latency": ([_P, _I, ctypes.POINTER(ctypes.c_double)], _I),
+    "se_server_get_grid": ([_P, _I, _P, ctypes.c_size_t], _I),
+    "se_server_get_frame": ([_P, _I, ctypes.POINTER(ctypes.c_int32)], _I),
     "se_world_read_timing": ([_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                               ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)], _I),
 }

@@ -12,6 +12,7 @@
 #include "lang/lang.hpp"
 #include "runtime/batch.hpp"
 #include "runtime/engine.hpp"
+#include "runtime/server.hpp"
 
 #define SE_API extern "C" __attribute__((visibility("default")))
 
@@ -437,6 +438,96 @@ SE_API int se_batch_info(const se_batch* b, int* resident_worlds, int* tiled_wor
     if (tiled_worlds) *tiled_worlds = (int)b->b->tiled.size();
     if (cells) *cells = b->b->cells;
     if (steps_per_launch) *steps_per_launch = b->b->variant ? b->b->variant->kmax : 0;
+    return (int)SE_OK;
+  });
+}
+
+// ---- serving -----------------------------------------------------------------------------
+struct se_server {
+  std::unique_ptr<se::rt::Server> s;
+};
+
+SE_API int se_server_create(se_ruleset* rs, long long budget_bytes, se_server** out) {
+  return guard([&] {
+    if (!rs || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    auto s = std::make_unique<se::rt::Server>();
+    se::rt::Status st = s->create(rs->rs, budget_bytes);
+    if (!st.ok()) return ret(st);
+    *out = new se_server{std::move(s)};
+    return (int)SE_OK;
+  });
+}
+
+SE_API void se_server_destroy(se_server* s) { delete s; }
+
+SE_API int se_server_set_frames_per_iteration(se_server* s, int k) {
+  return guard([&] {
+    if (!s) return fail(SE_ERR_INVALID_ARGUMENT, "null server");
+    return ret(s->s->set_frames_per_iteration(k));
+  });
+}
+
+SE_API int se_server_open_session(se_server* s, int width, int height, const uint32_t* cells, int32_t frame,
+                                  int* session) {
+  return guard([&] {
+    if (!s || !session) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(s->s->open_session(width, height, cells, frame, session));
+  });
+}
+
+SE_API int se_server_close_session(se_server* s, int session) {
+  return guard([&] {
+    if (!s) return fail(SE_ERR_INVALID_ARGUMENT, "null server");
+    return ret(s->s->close_session(session));
+  });
+}
+
+SE_API int se_server_submit(se_server* s, int session, int nframes, const se_modification* mods, int nmods,
+                            double arrival_ms, int* request) {
+  return guard([&] {
+    if (!s || !request) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(s->s->submit(session, nframes, mods, nmods, arrival_ms, request));
+  });
+}
+
+SE_API int se_server_run(se_server* s, int plain) {
+  return guard([&] {
+    if (!s) return fail(SE_ERR_INVALID_ARGUMENT, "null server");
+    return ret(s->s->run(plain != 0));
+  });
+}
+
+SE_API int se_server_stats_get(se_server* s, se_server_stats* out) {
+  return guard([&] {
+    if (!s || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(s->s->stats(out));
+  });
+}
+
+SE_API int se_server_request_latency(se_server* s, int request, double* latency_ms) {
+  return guard([&] {
+    if (!s || !latency_ms || request < 0 || request >= (int)s->s->requests.size())
+      return fail(SE_ERR_INVALID_ARGUMENT, "bad request");
+    const auto& r = s->s->requests[(size_t)request];
+    if (r.done_ms < 0) return fail(SE_ERR_INVALID_ARGUMENT, "request has not been served");
+    *latency_ms = r.done_ms - r.arrival_ms;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_server_get_grid(se_server* s, int session, uint32_t* cells, size_t count) {
+  return guard([&] {
+    if (!s || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(s->s->get_grid(session, cells, count));
+  });
+}
+
+SE_API int se_server_get_frame(se_server* s, int session, int32_t* frame) {
+  return guard([&] {
+    if (!s || !frame || session < 0 || session >= (int)s->s->sessions.size())
+      return fail(SE_ERR_INVALID_ARGUMENT, "bad session");
+    *frame = s->s->sessions[(size_t)session].frame;
     return (int)SE_OK;
   });
 }

@@ -356,6 +356,28 @@ __device__ __forceinline__ void se_mtile_impl(const SeWorldDesc* __restrict__ wo
   se_tile_run<TW, TH, KMAX, NT>(src, dst, w.W, w.H, w.frame + 1 + frames_done, k, lut, job.x0, job.y0);
 }
 
+// One serving iteration: descs[a] is the a-th active world, with its frames for this
+// iteration in pad0 (1..KMAX); prefix[a] is the first CTA of world a (prefix[n] = grid).
+// Each world reads its current buffer and writes the other one.
+template <int TW, int TH, int KMAX, int NT>
+__device__ __forceinline__ void se_stile_impl(const SeWorldDesc* __restrict__ descs, const int* __restrict__ prefix,
+                                              int nactive, const uint16_t* __restrict__ lut) {
+  const int t = blockIdx.x;
+  int lo = 0, hi = nactive - 1;  // last a with prefix[a] <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const SeWorldDesc w = descs[lo];
+  const int local = t - prefix[lo];
+  const int tiles_x = (w.W + TW - 1) / TW;
+  const int ty = local / tiles_x, tx = local - ty * tiles_x;
+  const uint32_t* src = w.cur ? w.buf1 : w.buf0;
+  uint32_t* dst = w.cur ? w.buf0 : w.buf1;
+  se_tile_run<TW, TH, KMAX, NT>(src, dst, w.W, w.H, w.frame + 1, w.pad0, lut, tx * TW, ty * TH);
+}
+
 // Whole-world launch: CTA b holds world ids[b] entirely in shared memory (plus a WALL
 // border: 4 columns each side for aligned loads, 1 row above and below), advances it by
 // `frames` frames and stores it to the buffer cur ^ out_flip.  Nothing outside the world is

@@ -186,10 +186,15 @@ Status World::timing_read(double* ms, long long* launches, long long* cell_frame
 }
 
 Status World::launch_edit(const se_modification* mods, int nlive) {
+  return launch_edit_on(*rs, buf[cur], W, H, mods, nlive, stream);
+}
+
+Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int H, const se_modification* mods, int nlive,
+                      cudaStream_t stream) {
   EditParams p;
   memset(&p, 0, sizeof p);
   long long total = 0;
-  const int nmat = rs->num_materials();
+  const int nmat = rs.num_materials();
   for (int i = 0; i < nlive; ++i) {
     const se_modification& m = mods[i];
     int* r = &p.mods[8 * i];
@@ -226,12 +231,12 @@ Status World::launch_edit(const se_modification* mods, int nlive) {
   }
   p.start[nlive] = total;
   if (total == 0) return Status::Ok();
-  cudaKernel_t kern = rs->module->get("se_edit");
-  uint32_t* g = buf[cur];
+  cudaKernel_t kern = rs.module->get("se_edit");
+  uint32_t* g = grid;
   int Wv = W, Hv = H, n = nlive;
   void* args[] = {(void*)&g, &Wv, &Hv, &n, &total, &p};
-  dim3 grid((unsigned)((total + 255) / 256));
-  SE_CUDA(cudaLaunchKernel((const void*)kern, grid, dim3(256), args, 0, stream));
+  dim3 blocks((unsigned)((total + 255) / 256));
+  SE_CUDA(cudaLaunchKernel((const void*)kern, blocks, dim3(256), args, 0, stream));
   return Status::Ok();
 }
 

@@ -85,6 +85,10 @@ struct World {
   Status histogram(unsigned long long* counts, int nbins);
 };
 
+// The edit pass (se_edit) for `nlive` mods over a W x H grid.
+Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int H, const se_modification* mods, int nlive,
+                      cudaStream_t stream);
+
 cudaError_t grid_digest(const uint32_t* g, unsigned long long n, unsigned long long* d_out, cudaStream_t s);
 cudaError_t grid_histogram(const uint32_t* g, unsigned long long n, int nbins, unsigned long long* d_counts,
                            cudaStream_t s);

@@ -44,8 +44,17 @@ std::string kernel_source(const std::string& generated_rules) {
          " int frames_done, int k, const uint16_t* __restrict__ lut) {\n"
       << "  se_mtile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
       << ">(worlds, jobs, pass, frames_done, k, lut);\n}\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(" << t.nt << ") " << t.serve_name()
+      << "(const SeWorldDesc* __restrict__ descs, const int* __restrict__ prefix, int nactive,"
+         " const uint16_t* __restrict__ lut) {\n"
+      << "  se_stile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
+      << ">(descs, prefix, nactive, lut);\n}\n";
   }
   return o.str();
+}
+
+std::string TileVariant::serve_name() const {
+  return "se_stile_" + std::to_string(tw) + "x" + std::to_string(th) + "_k" + std::to_string(kmax);
 }
 
 std::string TileVariant::multi_name() const {
@@ -164,6 +173,7 @@ bool Module::load(const std::string& cubin, unsigned long long lut_entries, std:
   for (auto& t : tile_variants()) {
     names.push_back(t.name());
     names.push_back(t.multi_name());
+    names.push_back(t.serve_name());
   }
   for (auto& n : names) {
     cudaKernel_t k;
@@ -175,7 +185,7 @@ bool Module::load(const std::string& cubin, unsigned long long lut_entries, std:
     kernels[n] = k;
   }
   for (auto& t : tile_variants()) {
-    for (const std::string& n : {t.name(), t.multi_name()}) {
+    for (const std::string& n : {t.name(), t.multi_name(), t.serve_name()}) {
       e = cudaFuncSetAttribute((const void*)kernels[n], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)tile_smem_bytes(t, lut_entries));
       if (e != cudaSuccess) {

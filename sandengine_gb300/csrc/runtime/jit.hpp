@@ -15,6 +15,7 @@ struct TileVariant {
   int tw, th, kmax, nt;
   std::string name() const;        // single-world kernel
   std::string multi_name() const;  // many-world (tile job list) kernel
+  std::string serve_name() const;  // serving iteration kernel (per-world frame counts)
   int halo_x() const { return ((kmax + 3) / 4) * 4; }
   int halo_y() const { return kmax; }
   size_t smem_bytes() const { return (size_t)(tw + 2 * halo_x()) * (size_t)(th + 2 * halo_y()); }

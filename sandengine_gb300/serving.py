@@ -1,0 +1,89 @@
+"""Serving simulation sessions with continuous batching (no counterpart in the reference).
+
+    srv = Server(ruleset, budget_bytes=150 << 30)
+    s = srv.open_session(w, h, cells=None, frame=1)
+    r = srv.submit(s, nframes=300, mods=[SimModification(...)], arrival_ms=12.5)
+    srv.run()              # continuous batching; srv.run(plain=True): one request at a time
+    srv.stats()            # p50/p99 latency, throughput, evictions
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+
+from ._lib import check, lib
+from .lang import Ruleset
+from .simulation import SimModification, mods_to_c
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("requests", ctypes.c_longlong), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("wall_ms", ctypes.c_double),
+                ("cell_updates", ctypes.c_double), ("iterations", ctypes.c_longlong),
+                ("evictions", ctypes.c_longlong), ("restores", ctypes.c_longlong),
+                ("peak_resident_bytes", ctypes.c_longlong)]
+
+
+class Server:
+    def __init__(self, ruleset: Ruleset, budget_bytes: int, frames_per_iteration: int = 8):
+        self.ruleset = ruleset
+        h = ctypes.c_void_p()
+        check(lib().se_server_create(ruleset.handle, int(budget_bytes), ctypes.byref(h)))
+        self._h = h
+        self.sizes = []
+        self.set_frames_per_iteration(frames_per_iteration)
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            lib().se_server_destroy(h)
+
+    def set_frames_per_iteration(self, k: int) -> None:
+        check(lib().se_server_set_frames_per_iteration(self._h, int(k)))
+
+    def open_session(self, width: int, height: int, cells: Optional[np.ndarray] = None, frame: int = 0) -> int:
+        sid = ctypes.c_int()
+        ptr = None
+        if cells is not None:
+            cells = np.ascontiguousarray(cells, dtype=np.uint32)
+            assert cells.shape == (height, width)
+            ptr = cells.ctypes.data
+        check(lib().se_server_open_session(self._h, int(width), int(height), ptr, int(frame), ctypes.byref(sid)))
+        self.sizes.append((int(width), int(height)))
+        return sid.value
+
+    def close_session(self, session: int) -> None:
+        check(lib().se_server_close_session(self._h, int(session)))
+
+    def submit(self, session: int, nframes: int, mods: Sequence[SimModification] = (), arrival_ms: float = 0.0) -> int:
+        rid = ctypes.c_int()
+        arr = mods_to_c(mods)
+        check(lib().se_server_submit(self._h, int(session), int(nframes), arr if len(mods) else None, len(mods),
+                                     float(arrival_ms), ctypes.byref(rid)))
+        return rid.value
+
+    def run(self, plain: bool = False) -> None:
+        check(lib().se_server_run(self._h, 1 if plain else 0))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib().se_server_stats_get(self._h, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in ServerStats._fields_}
+
+    def latency_ms(self, request: int) -> float:
+        v = ctypes.c_double()
+        check(lib().se_server_request_latency(self._h, int(request), ctypes.byref(v)))
+        return v.value
+
+    def grid(self, session: int) -> np.ndarray:
+        w, h = self.sizes[session]
+        out = np.empty((h, w), dtype=np.uint32)
+        check(lib().se_server_get_grid(self._h, int(session), out.ctypes.data, out.size))
+        return out
+
+    def frame(self, session: int) -> int:
+        f = ctypes.c_int32()
+        check(lib().se_server_get_frame(self._h, int(session), ctypes.byref(f)))
+        return f.value

@@ -51,6 +51,13 @@ extern "C" void emu_mtile_##TW##x##TH##_k##K(const SeWorldDesc* worlds, const Se
   } \
 }
 @MTILES@
+extern "C" void emu_stile_128x64_k8(const SeWorldDesc* descs, const int* prefix, int n) {
+  blockDim.x = 1; threadIdx.x = 0;
+  for (int t = 0; t < prefix[n]; ++t) {
+    blockIdx.x = t;
+    se_stile_impl<128, 64, 8, 1>(descs, prefix, n, g_lut);
+  }
+}
 extern "C" void emu_resident(const SeWorldDesc* worlds, const int* ids, int nids, int frames, int flip) {
   blockDim.x = 1; threadIdx.x = 0;
   for (int j = 0; j < nids; ++j) {
@@ -149,6 +156,26 @@ class Emu:
         self.lib.emu_finalize(desc.ctypes.data, n, F, P)
         out = [bufs[i][int(desc[i]["cur"])] for i in range(n)]
         return out, [int(f) for f in desc["frame"]]
+
+    def serve_iteration(self, grids, frames, ks):
+        """One serving iteration (128x64 tiles, up to 8 frames): world a advances ks[a]
+        frames from counter frames[a].  Returns the new grids."""
+        n = len(grids)
+        desc = np.zeros(n, dtype=[("b0", "<u8"), ("b1", "<u8"), ("W", "<i4"), ("H", "<i4"), ("frame", "<i4"),
+                                  ("cur", "<i4"), ("k", "<i4"), ("p1", "<i4")])
+        outs, prefix, total = [], [], 0
+        for a, g in enumerate(grids):
+            src = np.ascontiguousarray(g, dtype=np.uint32)
+            dst = np.zeros_like(src)
+            outs.append((src, dst))
+            desc[a] = (src.ctypes.data, dst.ctypes.data, g.shape[1], g.shape[0], frames[a], 0, ks[a], 0)
+            prefix.append(total)
+            total += ((g.shape[1] + 127) // 128) * ((g.shape[0] + 63) // 64)
+        prefix.append(total)
+        pre = np.array(prefix, dtype=np.int32)
+        self.lib.emu_stile_128x64_k8.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        self.lib.emu_stile_128x64_k8(desc.ctypes.data, pre.ctypes.data, n)
+        return [o[1] for o in outs]
 
     def edit(self, grid: np.ndarray, mods) -> None:
         """The edit pass in place; host-side preparation as in runtime/engine.cpp."""

@@ -58,6 +58,21 @@ def test_batch_kernels_match_port(emus, ports, name):
             assert fr[i] == frames0[i] + F
 
 
+def test_serving_iteration_matches_port(emus, ports):
+    """One launch advancing several worlds by different frame counts."""
+    name = "twelve_materials"
+    E, P = emus[name], ports[name]
+    sizes = [(300, 200), (64, 64), (129, 65), (5, 300)]
+    grids = [_world(name, w, h, 20 + i) for i, (w, h) in enumerate(sizes)]
+    frames = [3, 10, 1, 7]
+    ks = [8, 1, 5, 3]
+    outs = E.serve_iteration(grids, frames, ks)
+    for g, f, k, o in zip(grids, frames, ks, outs):
+        want = g.copy()
+        P.run(want, f, k)
+        assert np.array_equal(o, want)
+
+
 @pytest.mark.parametrize("name", ["reference", "twelve_materials"])
 def test_edit_pass_matches_port(emus, ports, name):
     w, h = 300, 200
