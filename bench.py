@@ -46,7 +46,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="world16384",
-                    choices=["world16384", "world8192", "world4096", "world256", "batch4096"])
+                    choices=["world16384", "world8192", "world4096", "world256", "batch4096", "serve"])
     ap.add_argument("--worlds", type=int, default=4096, help="batch4096: number of worlds")
     ap.add_argument("--k", type=int, default=0, help="frames per launch (0 = autotuned)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
@@ -385,6 +385,71 @@ def run_batch(args, rep):
     }
 
 
+def serve_workload(rate, n_requests, seed=5):
+    """Poisson arrivals at `rate` req/s; each request opens a new session (p=0.5) or reuses an
+    earlier one; sides log-uniform in [128, 2048] (multiples of 32); N ~ U[1, 600] frames;
+    0-8 circle edits (radius 8-64, EMPTY or sand) on the first frame."""
+    from sandengine_gb300 import workloads as wl
+    u = wl.uniform53(seed, 9, np.arange(8 * n_requests, dtype=np.uint64)).astype(np.float64) / float(1 << 53)
+    u = u.reshape(n_requests, 8)
+    t = np.cumsum(-np.log1p(-u[:, 0]) / rate) * 1e3  # ms
+    sessions, reqs = [], []
+    for i in range(n_requests):
+        if not sessions or u[i, 1] < 0.5:
+            w = int(np.clip(np.round(np.exp(np.log(128) + u[i, 2] * np.log(16)) / 32) * 32, 128, 2048))
+            h = int(np.clip(np.round(np.exp(np.log(128) + u[i, 3] * np.log(16)) / 32) * 32, 128, 2048))
+            sessions.append((w, h))
+            s = len(sessions) - 1
+        else:
+            s = int(u[i, 1] * 2 * len(sessions)) % len(sessions)
+        n = 1 + int(u[i, 4] * 600)
+        ne = int(u[i, 5] * 9)
+        w, h = sessions[s]
+        mods = wl.circle_edits(w, h, seed, i, ne, [0, 3]) if ne else []
+        reqs.append((s, n, mods, float(t[i])))
+    return sessions, reqs
+
+
+def run_serve(args, rep):
+    import sandengine_gb300 as se
+    from sandengine_gb300 import workloads as wl
+    from sandengine_gb300.serving import Server
+    rs = se.parse_string(wl.ruleset_text("twelve_materials"))
+    spec = wl.twelve_fill_spec()
+    budget = 150 << 30
+    sweep = []
+    for rate in (200, 1000, 4000, 16000):
+        n_req = int(min(1200, max(200, rate * 0.6)))
+        sessions, reqs = serve_workload(rate, n_req)
+        grids = [wl.patch_fill(w, h, 3000 + i, *spec, patch=64) for i, (w, h) in enumerate(sessions)]
+        row = {"rate_req_s": rate, "requests": n_req, "sessions": len(sessions)}
+        for mode in ("batched", "plain"):
+            srv = Server(rs, budget)
+            for (w, h), g in zip(sessions, grids):
+                srv.open_session(w, h, g, 1)
+            for (s, n, mods, t) in reqs:
+                srv.submit(s, n, [se.SimModification((m[0], m[1]), m[2], m[3], m[4]) for m in mods], t)
+            srv.run(plain=(mode == "plain"))
+            st = srv.stats()
+            row[mode] = {"throughput": st["cell_updates"] / (st["wall_ms"] / 1e3), "p50_ms": st["p50_ms"],
+                         "p99_ms": st["p99_ms"], "wall_ms": st["wall_ms"], "iterations": st["iterations"],
+                         "evictions": st["evictions"]}
+            del srv
+        row["speedup"] = row["batched"]["throughput"] / row["plain"]["throughput"]
+        sweep.append(row)
+    best = max(sweep, key=lambda r: r["batched"]["throughput"])
+    return {
+        "metric": METRIC, "value": best["batched"]["throughput"], "unit": UNIT, "n_gpus": rep.world_size,
+        "steps": len(sweep), "warmup": 0, "ms_per_step": best["batched"]["wall_ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded splitmix64)",
+        "config": {"workload": "serve: Poisson arrivals (200-16000 req/s), sides log-uniform in [128, 2048], "
+                               "N ~ U[1, 600] frames, 0-8 circle edits, twelve_materials rule set, 150 GB budget; "
+                               "continuous batching vs one request at a time",
+                   "parallelism": f"replicas{rep.world_size}"},
+        "serving": sweep,
+    }
+
+
 def run_reference(args, rep):
     if rep.rank != 0:
         return None
@@ -438,6 +503,8 @@ def main():
             out = run_reference(args, rep)
         elif args.workload.startswith("batch"):
             out = run_batch(args, rep)
+        elif args.workload == "serve":
+            out = run_serve(args, rep)
         else:
             out = run_ours(args, rep)
         if rep.rank == 0 and out is not None:
