@@ -236,6 +236,19 @@ int se_server_request_latency(se_server* s, int request, double* latency_ms);
 int se_server_get_grid(se_server* s, int session, uint32_t* cells, size_t count);
 int se_server_get_frame(se_server* s, int session, int32_t* frame);
 
+/* ---- world snapshots (the reference lists world saving/loading as a TODO, README.md:85-87) */
+/* A snapshot file holds a world's whole state: its grid and frame counter, plus the size,
+ * the number of materials and a fingerprint of the rule set it was saved with (loading
+ * under a different rule set is refused).  Layout: 32-byte little-endian header ("SEW1",
+ * header size, width, height, frame, materials, u64 rule-set fingerprint), then the cells. */
+int se_snapshot_info(const char* path, int* width, int* height, int32_t* frame);
+int se_world_save(se_world* w, const char* path);
+/* The snapshot's size must equal the world's. */
+int se_world_load(se_world* w, const char* path);
+/* The same format for serving sessions (an evicted session is this record in host memory). */
+int se_server_save_session(se_server* s, int session, const char* path);
+int se_server_open_session_from(se_server* s, const char* path, int* session);
+
 #ifdef __cplusplus
 }
 #endif

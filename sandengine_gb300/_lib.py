@@ -102,6 +102,12 @@ _SIGS = {
     "se_server_request_latency": ([_P, _I, ctypes.POINTER(ctypes.c_double)], _I),
     "se_server_get_grid": ([_P, _I, _P, ctypes.c_size_t], _I),
     "se_server_get_frame": ([_P, _I, ctypes.POINTER(ctypes.c_int32)], _I),
+    "se_snapshot_info": ([ctypes.c_char_p, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_int32)],
+                         _I),
+    "se_world_save": ([_P, ctypes.c_char_p], _I),
+    "se_world_load": ([_P, ctypes.c_char_p], _I),
+    "se_server_save_session": ([_P, _I, ctypes.c_char_p], _I),
+    "se_server_open_session_from": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
     "se_world_read_timing": ([_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                               ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)], _I),
 }

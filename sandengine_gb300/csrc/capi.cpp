@@ -13,6 +13,7 @@
 #include "runtime/batch.hpp"
 #include "runtime/engine.hpp"
 #include "runtime/server.hpp"
+#include "runtime/snapshot.hpp"
 
 #define SE_API extern "C" __attribute__((visibility("default")))
 
@@ -520,6 +521,99 @@ SE_API int se_server_get_grid(se_server* s, int session, uint32_t* cells, size_t
   return guard([&] {
     if (!s || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
     return ret(s->s->get_grid(session, cells, count));
+  });
+}
+
+// ---- snapshots ---------------------------------------------------------------------------
+namespace {
+se::rt::SnapshotHeader snapshot_header_for(const se::rt::Ruleset& rs, int W, int H, int32_t frame) {
+  se::rt::SnapshotHeader h;
+  h.width = (uint32_t)W;
+  h.height = (uint32_t)H;
+  h.frame = frame;
+  h.num_materials = (uint32_t)rs.num_materials();
+  h.ruleset_hash = se::rt::ruleset_fingerprint(rs.materials_glsl, rs.rules_glsl);
+  return h;
+}
+int check_snapshot_matches(const se::rt::Ruleset& rs, const se::rt::SnapshotHeader& h) {
+  if (h.num_materials != (uint32_t)rs.num_materials() ||
+      h.ruleset_hash != se::rt::ruleset_fingerprint(rs.materials_glsl, rs.rules_glsl))
+    return fail(SE_ERR_INVALID_ARGUMENT, "the snapshot was saved with a different rule set");
+  return (int)SE_OK;
+}
+}  // namespace
+
+SE_API int se_snapshot_info(const char* path, int* width, int* height, int32_t* frame) {
+  return guard([&] {
+    if (!path) return fail(SE_ERR_INVALID_ARGUMENT, "null path");
+    se::rt::SnapshotHeader h;
+    std::string err;
+    if (!se::rt::snapshot_read_header(path, &h, &err)) return fail(SE_ERR_INVALID_ARGUMENT, err);
+    if (width) *width = (int)h.width;
+    if (height) *height = (int)h.height;
+    if (frame) *frame = h.frame;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_save(se_world* w, const char* path) {
+  return guard([&] {
+    if (!w || !path) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    auto& W = *w->w;
+    std::vector<uint32_t> cells((size_t)W.W * W.H);
+    int rc = grid_copy(w, cells.data(), cells.size(), false, true);
+    if (rc) return rc;
+    std::string err;
+    if (!se::rt::snapshot_write(path, snapshot_header_for(*W.rs, W.W, W.H, W.frame), cells.data(), &err))
+      return fail(SE_ERR_INVALID_ARGUMENT, err);
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_load(se_world* w, const char* path) {
+  return guard([&] {
+    if (!w || !path) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    auto& W = *w->w;
+    se::rt::SnapshotHeader h;
+    std::vector<uint32_t> cells;
+    std::string err;
+    if (!se::rt::snapshot_read(path, &h, &cells, &err)) return fail(SE_ERR_INVALID_ARGUMENT, err);
+    if ((int)h.width != W.W || (int)h.height != W.H)
+      return fail(SE_ERR_INVALID_ARGUMENT, "the snapshot's size differs from the world's");
+    int rc = check_snapshot_matches(*W.rs, h);
+    if (rc) return rc;
+    rc = grid_copy(w, cells.data(), cells.size(), true, true);
+    if (rc) return rc;
+    W.frame = h.frame;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_server_save_session(se_server* s, int session, const char* path) {
+  return guard([&] {
+    if (!s || !path || session < 0 || session >= (int)s->s->sessions.size())
+      return fail(SE_ERR_INVALID_ARGUMENT, "bad argument");
+    const auto& ss = s->s->sessions[(size_t)session];
+    std::vector<uint32_t> cells((size_t)ss.W * ss.H);
+    se::rt::Status st = s->s->get_grid(session, cells.data(), cells.size());
+    if (!st.ok()) return ret(st);
+    std::string err;
+    if (!se::rt::snapshot_write(path, snapshot_header_for(*s->s->rs, ss.W, ss.H, ss.frame), cells.data(), &err))
+      return fail(SE_ERR_INVALID_ARGUMENT, err);
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_server_open_session_from(se_server* s, const char* path, int* session) {
+  return guard([&] {
+    if (!s || !path || !session) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    se::rt::SnapshotHeader h;
+    std::vector<uint32_t> cells;
+    std::string err;
+    if (!se::rt::snapshot_read(path, &h, &cells, &err)) return fail(SE_ERR_INVALID_ARGUMENT, err);
+    int rc = check_snapshot_matches(*s->s->rs, h);
+    if (rc) return rc;
+    return ret(s->s->open_session((int)h.width, (int)h.height, cells.data(), h.frame, session));
   });
 }
 

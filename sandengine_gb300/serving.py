@@ -54,6 +54,17 @@ class Server:
         self.sizes.append((int(width), int(height)))
         return sid.value
 
+    def save_session(self, session: int, path: str) -> None:
+        check(lib().se_server_save_session(self._h, int(session), str(path).encode()))
+
+    def open_session_from(self, path: str) -> int:
+        from .simulation import snapshot_info
+        info = snapshot_info(path)
+        sid = ctypes.c_int()
+        check(lib().se_server_open_session_from(self._h, str(path).encode(), ctypes.byref(sid)))
+        self.sizes.append((info["width"], info["height"]))
+        return sid.value
+
     def close_session(self, session: int) -> None:
         check(lib().se_server_close_session(self._h, int(session)))
 

@@ -14,6 +14,7 @@ Extensions over the reference: ``run_frames(n, mods)`` advances n frames in one 
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence, Tuple
 
@@ -127,6 +128,14 @@ class Simulation:
         check(lib().se_world_device_grid(self._h, ctypes.byref(p)))
         return p.value or 0
 
+    def save(self, path: str) -> None:
+        """Write the world's grid and frame counter to a snapshot file."""
+        check(lib().se_world_save(self._h, os.fspath(path).encode()))
+
+    def load(self, path: str) -> None:
+        """Replace the grid and frame counter from a snapshot of the same size and rule set."""
+        check(lib().se_world_load(self._h, os.fspath(path).encode()))
+
     def autotune(self, reps: int = 3) -> int:
         """Pick the fastest tile shape / frames per launch for this world (state unchanged);
         returns the chosen frames per launch."""
@@ -156,6 +165,13 @@ class Simulation:
         out = np.zeros(n, dtype=np.uint64)
         check(lib().se_world_histogram(self._h, out.ctypes.data, n))
         return out
+
+
+def snapshot_info(path: str) -> dict:
+    """Size and frame counter stored in a snapshot file (no GPU needed)."""
+    w, h, f = ctypes.c_int(), ctypes.c_int(), ctypes.c_int32()
+    check(lib().se_snapshot_info(os.fspath(path).encode(), ctypes.byref(w), ctypes.byref(h), ctypes.byref(f)))
+    return {"width": w.value, "height": h.value, "frame": f.value}
 
 
 def grid_digest(grid: np.ndarray) -> int:
