@@ -91,6 +91,14 @@ int se_ruleset_compile(se_ruleset* rs);
 int se_ruleset_num_materials(const se_ruleset* rs, int* n);
 /* Material id by name (materials.rs ids), or SE_ERR_NOT_FOUND. */
 int se_ruleset_material_id(const se_ruleset* rs, const char* name, int* id);
+/* The block transition table this device built for the rule set (no counterpart in the
+ * reference, whose shader evaluates the rules per block; this is introspection for
+ * tests).  *entries gets the number of u16 entries and *static_words the 32-bit words of
+ * the bitset of static keys (both 0 when the rules need the direct path); when `table` /
+ * `bits` are not null, at most cap_entries / cap_words of them are copied from the device.
+ * Loads the kernels on the current device first. */
+int se_ruleset_table(se_ruleset* rs, uint16_t* table, size_t cap_entries, uint32_t* bits, size_t cap_words,
+                     unsigned long long* entries, unsigned long long* static_words);
 void se_ruleset_free(se_ruleset* rs);
 
 /* ---- one world (replaces sandengine-core::simulation::Simulation) --------------------- */

@@ -128,6 +128,31 @@ SE_API int se_ruleset_compile(se_ruleset* rs) {
   });
 }
 
+SE_API int se_ruleset_table(se_ruleset* rs, uint16_t* table, size_t cap_entries, uint32_t* bits, size_t cap_words,
+                            unsigned long long* entries, unsigned long long* static_words) {
+  return guard([&] {
+    if (!rs || !entries || !static_words) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    se::rt::Ruleset& r = *rs->rs;
+    se::rt::Status s = r.ensure_loaded();
+    if (!s.ok()) return ret(s);
+    *entries = r.cuda.lut_entries;
+    *static_words = r.cuda.lut_static_words;
+    if (!r.d_lut) return (int)SE_OK;
+    if (table) {
+      const size_t n = (size_t)std::min<unsigned long long>(cap_entries, r.cuda.lut_entries);
+      cudaError_t e = cudaMemcpy(table, r.d_lut, n * sizeof(uint16_t), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    }
+    if (bits) {
+      const size_t off = ((size_t)r.cuda.lut_entries * sizeof(uint16_t) + 15) & ~(size_t)15;
+      const size_t n = (size_t)std::min<unsigned long long>(cap_words, r.cuda.lut_static_words);
+      cudaError_t e = cudaMemcpy(bits, reinterpret_cast<const char*>(r.d_lut) + off, n * 4, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    }
+    return (int)SE_OK;
+  });
+}
+
 SE_API int se_ruleset_num_materials(const se_ruleset* rs, int* n) {
   return guard([&] {
     if (!rs || !n) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");

@@ -84,6 +84,34 @@ extern "C" __global__ void __launch_bounds__(256) se_build_lut(uint16_t* __restr
 }
 // Tables up to this size are copied into shared memory by each CTA.
 #define SE_LUT_SMEM_MAX_ENTRIES 16384u
+#if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
+#define SE_LUT_SMEM_BYTES ((SE_LUT_ENTRIES * 2u + 15u) & ~15u)
+#else
+#define SE_LUT_SMEM_BYTES 0u
+#endif
+// The bitset of static keys follows the table at this byte offset.  Bit `key` is set when
+// the table maps the block with that key to itself for every hash value.
+#define SE_LUT_STATIC_OFF ((SE_LUT_ENTRIES * 2u + 15u) & ~15u)
+
+// Fills the static-key bitset after se_build_lut, one thread per 32-bit word.  Table
+// indices are key * C + hash class (se_gen::lut_index), so a key's entries are contiguous.
+extern "C" __global__ void __launch_bounds__(256) se_build_static(uint16_t* __restrict__ lut) {
+  constexpr uint32_t C = SE_LUT_ENTRIES / SE_LUT_KEYS, M = (1u << SE_LUT_BITS) - 1u;
+  uint32_t* st = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(lut) + SE_LUT_STATIC_OFF);
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= SE_LUT_STATIC_WORDS) return;
+  uint32_t word = 0;
+  for (uint32_t j = 0; j < 32u && w * 32u + j < SE_LUT_KEYS; ++j) {
+    const uint32_t key = w * 32u + j;
+    const uint32_t a = key & M, b = (key >> SE_LUT_BITS) & M, c = (key >> (2 * SE_LUT_BITS)) & M,
+                   d = (key >> (3 * SE_LUT_BITS)) & M;
+    const uint32_t self = a | (b << 4) | (c << 8) | (d << 12);
+    bool same = true;
+    for (uint32_t q = 0; q < C; ++q) same = same && lut[key * C + q] == self;
+    if (same) word |= 1u << j;
+  }
+  st[w] = word;
+}
 #endif
 
 // One block's update: the block transition table when the rule set has one, else the
@@ -146,6 +174,168 @@ __device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int 
     se_block_store(p, SW, a, b, c, d, gx, gy, W, H, edge);
   }
 }
+
+#ifdef SE_LUT
+// Interior tiles with a block transition table run each step in two phases over chunks of
+// four horizontally adjacent blocks (8 cells x 2 rows):
+//  1. se_chunk_collect reads every chunk with two 8-byte loads.  A chunk whose 16 cells are
+//     one material m, where the table never changes the block of four m cells (EMPTY, and
+//     in a typical rule set the solids and liquids at rest), is left as it is; the others
+//     are appended to a list of array offsets (a warp reserves its slots with one
+//     atomicAdd).  The blocks of a row past its last whole chunk are updated right there.
+//  2. se_chunk_process updates the listed chunks, one chunk per thread, with word-wide
+//     shared-memory access.
+// Chunks are skipped whole, so the lanes that evaluate blocks do so together rather than
+// waiting on one another; blocks of one step are disjoint, so the list order is free.
+
+// Shared-memory layout after the cell array and the table copy: 16 bytes of slack (chunk
+// loads at odd offsets read up to 3 bytes past a row), the two list counters used by
+// alternate steps, one flag byte per material id < 16, then the list.
+#define SE_HDR_CNT 16
+#define SE_HDR_FLAGS 32
+#define SE_HDR_LIST 48
+
+// flags[m] = 1 when the block of four m cells is static (from se_build_static's bitset).
+__device__ __forceinline__ void se_uniform_flags(const uint16_t* __restrict__ lut, uint8_t* flags, int nt) {
+  const uint32_t* st = reinterpret_cast<const uint32_t*>(reinterpret_cast<const uint8_t*>(lut) + SE_LUT_STATIC_OFF);
+  for (uint32_t m = threadIdx.x; m < 16u; m += nt) {
+    uint32_t bit = 0;
+    if (m < SE_NMAT && m < (1u << SE_LUT_BITS)) {
+      const uint32_t key = se_gen::lut_key(m, m, m, m);
+      bit = (__ldg(st + (key >> 5)) >> (key & 31u)) & 1u;
+    }
+    flags[m] = (uint8_t)bit;
+  }
+}
+// The 16 flag bytes as a bit mask (bit m = flags[m]).
+__device__ __forceinline__ uint32_t se_flags_mask(const uint8_t* flags) {
+  const uint4 v = *reinterpret_cast<const uint4*>(flags);
+  // (w & 0x01010101) * 0x01020408 gathers the low bit of each byte into bits 24..27
+  const uint32_t m0 = ((v.x & 0x01010101u) * 0x01020408u) >> 24, m1 = ((v.y & 0x01010101u) * 0x01020408u) >> 24,
+                 m2 = ((v.z & 0x01010101u) * 0x01020408u) >> 24, m3 = ((v.w & 0x01010101u) * 0x01020408u) >> 24;
+  return (m0 & 15u) | ((m1 & 15u) << 4) | ((m2 & 15u) << 8) | ((m3 & 15u) << 12);
+}
+
+// 8 consecutive cells at p.  OX = 0: p is 8-byte aligned; OX = 1: one byte past that.
+template <int OX>
+__device__ __forceinline__ void se_ld8(const uint8_t* p, uint32_t& lo, uint32_t& hi) {
+  if (OX == 0) {
+    const uint2 v = *reinterpret_cast<const uint2*>(p);
+    lo = v.x;
+    hi = v.y;
+  } else {
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(p - 1);
+    const uint32_t w0 = q[0], w1 = q[1], w2 = q[2];
+    lo = __funnelshift_r(w0, w1, 8);
+    hi = __funnelshift_r(w1, w2, 8);
+  }
+}
+template <int OX>
+__device__ __forceinline__ void se_st8(uint8_t* p, uint32_t lo, uint32_t hi) {
+  if (OX == 0) {
+    *reinterpret_cast<uint2*>(p) = make_uint2(lo, hi);
+  } else {  // byte, half-word, word, byte
+    p[0] = (uint8_t)lo;
+    *reinterpret_cast<uint16_t*>(p + 1) = (uint16_t)(lo >> 8);
+    *reinterpret_cast<uint32_t*>(p + 3) = (lo >> 24) | (hi << 8);
+    p[7] = (uint8_t)(hi >> 24);
+  }
+}
+
+// Table lookup for a block given as the 4 bytes [a, b, c, d] (ids < 16) with hash base x;
+// returns the new block in the same layout.
+__device__ __forceinline__ uint32_t se_lut_word(uint32_t abcd, uint32_t x, const uint16_t* __restrict__ lut) {
+#if SE_LUT_BITS == 4
+  const uint32_t y = abcd | (abcd >> 4);  // byte 0 = a | b << 4, byte 2 = c | d << 4
+  const uint32_t key = (y & 0xffu) | ((y >> 8) & 0xff00u);
+#else
+  const uint32_t key = se_gen::lut_key(abcd & 0xffu, (abcd >> 8) & 0xffu, (abcd >> 16) & 0xffu, abcd >> 24);
+#endif
+  const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u), h3 = se_mix(x * 213132u);
+  const uint32_t idx = se_gen::lut_index_key(key, h0, h1, h2, h3);
+#if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
+  const uint32_t o = lut[idx];
+#else
+  const uint32_t o = __ldg(lut + idx);
+#endif
+  const uint32_t t = (o & 0xffu) | ((o << 8) & 0xff0000u);  // nibbles a b c d -> bytes
+  return (t | (t << 4)) & 0x0f0f0f0fu;
+}
+
+// Appends `entry` for the lanes with `dyn` set; every lane of the warp calls it.
+__device__ __forceinline__ void se_list_push(bool dyn, uint32_t entry, uint16_t* __restrict__ list,
+                                             int* __restrict__ cnt) {
+  const uint32_t m = __ballot_sync(0xffffffffu, dyn);
+  if (m == 0u) return;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(cnt, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (dyn) list[base + __popc(m & ((1u << lane) - 1u))] = (uint16_t)entry;
+}
+
+template <int SW, int SH, int OX, int NT>
+__device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int gx0, int gy0, int f, int W, int H,
+                                                 const uint16_t* __restrict__ lut, uint32_t umask,
+                                                 uint16_t* __restrict__ list, int* __restrict__ cnt) {
+  static_assert(NT % 32 == 0 || NT == 1, "whole warps");
+  static_assert(SW % 8 == 0 && SW * SH <= 65536, "8-byte rows, 16-bit offsets");
+  constexpr int NBX = (SW - OX) / 2, NCX = NBX / 4, REM = NBX - 4 * NCX;
+  const int nby = (SH - ly0) / 2;
+  const int nc = NCX * nby;
+  for (int base = threadIdx.x & ~31; base < nc; base += NT) {  // warp-uniform trip count
+    const int ci = base + (threadIdx.x & 31);
+    bool dyn = false;
+    int off = 0;
+    if (ci < nc) {
+      const int j = ci / NCX, q = ci - j * NCX;
+      off = (ly0 + 2 * j) * SW + OX + 8 * q;
+      uint32_t a0, a1, b0, b1;
+      se_ld8<OX>(sm + off, a0, a1);
+      se_ld8<OX>(sm + off + SW, b0, b1);
+      const uint32_t m = a0 & 0xffu;
+      const bool uniform = ((a0 ^ a1) | (a0 ^ b0) | (a0 ^ b1)) == 0u && a0 == m * 0x01010101u;
+      dyn = !(uniform && m < 16u && ((umask >> m) & 1u));
+    }
+    se_list_push(dyn, (uint32_t)off, list, cnt);
+  }
+  if (REM) {  // blocks past the last whole chunk of each row
+    for (int t = threadIdx.x; t < nby * REM; t += NT) {
+      const int j = t / REM, r = t - j * REM;
+      const int lx = OX + 2 * (4 * NCX + r), ly = ly0 + 2 * j;
+      uint8_t* p = sm + ly * SW + lx;
+      uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+      if ((a | b | c | d) == 0u) continue;
+      const int gx = gx0 + lx, gy = gy0 + ly;
+      se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
+      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, false);
+    }
+  }
+}
+
+template <int SW, int OX, int NT>
+__device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int gx0,
+                                                 int gy0, int f, const uint16_t* __restrict__ lut) {
+  const uint32_t xf = (uint32_t)f * 4541161u;
+  for (int i = threadIdx.x; i < n; i += NT) {
+    const int off = list[i];
+    const int ly = off / SW, lx = off - ly * SW;
+    uint8_t* p = sm + off;
+    uint32_t a0, a1, b0, b1;
+    se_ld8<OX>(p, a0, a1);
+    se_ld8<OX>(p + SW, b0, b1);
+    const uint32_t x = (uint32_t)(gx0 + lx) * 461u + (uint32_t)(gy0 + ly) * 2131u + xf;
+    uint32_t B0 = __byte_perm(a0, b0, 0x5410), B1 = __byte_perm(a0, b0, 0x7632);  // [a, b, c, d] per block
+    uint32_t B2 = __byte_perm(a1, b1, 0x5410), B3 = __byte_perm(a1, b1, 0x7632);
+    if (B0) B0 = se_lut_word(B0, x, lut);  // next block: origin x + 2
+    if (B1) B1 = se_lut_word(B1, x + 922u, lut);
+    if (B2) B2 = se_lut_word(B2, x + 1844u, lut);
+    if (B3) B3 = se_lut_word(B3, x + 2766u, lut);
+    se_st8<OX>(p, __byte_perm(B0, B1, 0x5410), __byte_perm(B2, B3, 0x5410));
+    se_st8<OX>(p + SW, __byte_perm(B0, B1, 0x7632), __byte_perm(B2, B3, 0x7632));
+  }
+}
+#endif
 
 // The same over a shared array whose size is only known at run time (whole worlds); the
 // block index is split with a float reciprocal and a +-1 correction.
@@ -266,6 +456,14 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   extern __shared__ __align__(16) uint8_t se_smem[];
   uint8_t* sm = se_smem;
   se_gen::init_tables(threadIdx.x, NT);
+#ifdef SE_LUT
+  constexpr int HDR = ((SW * SH + 15) & ~15) + (int)SE_LUT_SMEM_BYTES;
+  int* cnt = reinterpret_cast<int*>(se_smem + HDR + SE_HDR_CNT);
+  uint8_t* flags = se_smem + HDR + SE_HDR_FLAGS;
+  uint16_t* list = reinterpret_cast<uint16_t*>(se_smem + HDR + SE_HDR_LIST);
+  for (int i = threadIdx.x; i < 2; i += NT) cnt[i] = 0;
+  se_uniform_flags(lut, flags, NT);
+#endif
   lut = se_lut_to_smem(lut, se_smem, (SW * SH + 15) & ~15, NT);
   const int gx0 = X0 - HX, gy0 = Y0 - HY;
   const bool vec = (W & 3) == 0;
@@ -292,9 +490,30 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   __syncthreads();
 
   const bool edge = gx0 < 0 || gy0 < 0 || gx0 + SW > W || gy0 + SH > H;
+#ifdef SE_LUT
+  const uint32_t umask = se_flags_mask(flags);
+#endif
   for (int s = 0; s < k; ++s) {
     const int f = f0 + s;
     const int ly0 = (se_off_y(f) + gy0) & 1;  // gy0 = Y0 - HY is odd when HY is
+#ifdef SE_LUT
+    if (!edge) {
+      int* c = cnt + (s & 1);
+      if (se_off_x(f) == 0)
+        se_chunk_collect<SW, SH, 0, NT>(sm, ly0, gx0, gy0, f, W, H, lut, umask, list, c);
+      else
+        se_chunk_collect<SW, SH, 1, NT>(sm, ly0, gx0, gy0, f, W, H, lut, umask, list, c);
+      __syncthreads();
+      const int n = *c;
+      if (threadIdx.x == 0) cnt[(s + 1) & 1] = 0;  // last read in step s - 1
+      if (se_off_x(f) == 0)
+        se_chunk_process<SW, 0, NT>(sm, list, n, gx0, gy0, f, lut);
+      else
+        se_chunk_process<SW, 1, NT>(sm, list, n, gx0, gy0, f, lut);
+      __syncthreads();
+      continue;
+    }
+#endif
     if (se_off_x(f) == 0)
       se_tile_step<SW, SH, 0, NT>(sm, ly0, gx0, gy0, f, W, H, edge, lut);
     else

@@ -1090,11 +1090,15 @@ bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err) {
     uint64_t entries = 1ull << (4 * bits);
     for (int l = 0; l < 4; ++l) entries *= g.bounds[l].size() + 1;
     if (entries > (1ull << 24)) lut = false;
+    const uint64_t keys = 1ull << (4 * bits);
     if (lut) {
-      o << "#define SE_LUT 1\n#define SE_LUT_BITS " << bits << "\n#define SE_LUT_ENTRIES " << entries << "u\n";
-      o << "__device__ __forceinline__ uint32_t lut_index(uint32_t a, uint32_t b, uint32_t c, uint32_t d, "
-           "uint32_t h0, uint32_t h1, uint32_t h2, uint32_t h3) {\n"
-        << "  uint32_t i = a | (b << " << bits << ") | (c << " << 2 * bits << ") | (d << " << 3 * bits << ");\n";
+      o << "#define SE_LUT 1\n#define SE_LUT_BITS " << bits << "\n#define SE_LUT_ENTRIES " << entries << "u\n"
+        << "#define SE_LUT_KEYS " << keys << "u\n#define SE_LUT_STATIC_WORDS " << std::max<uint64_t>(1, keys / 32)
+        << "u\n";
+      o << "__device__ __forceinline__ uint32_t lut_key(uint32_t a, uint32_t b, uint32_t c, uint32_t d) {\n"
+        << "  return a | (b << " << bits << ") | (c << " << 2 * bits << ") | (d << " << 3 * bits << ");\n}\n";
+      o << "__device__ __forceinline__ uint32_t lut_index_key(uint32_t i, uint32_t h0, uint32_t h1, uint32_t h2, "
+           "uint32_t h3) {\n";
       for (int l = 0; l < 4; ++l) {
         if (g.bounds[l].empty()) continue;
         o << "  i = i * " << g.bounds[l].size() + 1 << "u";
@@ -1102,6 +1106,9 @@ bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err) {
         o << ";\n";
       }
       o << "  return i;\n}\n";
+      o << "__device__ __forceinline__ uint32_t lut_index(uint32_t a, uint32_t b, uint32_t c, uint32_t d, "
+           "uint32_t h0, uint32_t h1, uint32_t h2, uint32_t h3) {\n"
+        << "  return lut_index_key(lut_key(a, b, c, d), h0, h1, h2, h3);\n}\n";
       // decode: idx -> cells and one representative hash value per lane
       o << "__device__ __forceinline__ void lut_decode(uint32_t i, uint32_t& a, uint32_t& b, uint32_t& c, "
            "uint32_t& d, uint32_t& h0, uint32_t& h1, uint32_t& h2, uint32_t& h3) {\n"
@@ -1120,6 +1127,7 @@ bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err) {
     o << "}  // namespace se_gen\n";
     out->source = o.str();
     out->lut_entries = lut ? entries : 0;
+    out->lut_static_words = lut ? std::max<uint64_t>(1, keys / 32) : 0;
     out->num_materials = g.nmat;
     for (int i = 0; i < 4; ++i) out->uses_rand_lane[i] = g.uses_lane[i];
     return true;

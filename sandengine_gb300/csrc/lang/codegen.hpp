@@ -29,6 +29,9 @@ struct CudaRules {
   // evaluation path (they read positions / the frame, use rand as a number, or there are
   // more than 16 materials).
   unsigned long long lut_entries = 0;
+  // 32-bit words of the table's "static block" bitset (one bit per four-cell key: the block
+  // never changes, whatever the hash), stored after the table.
+  unsigned long long lut_static_words = 0;
 };
 
 bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err);

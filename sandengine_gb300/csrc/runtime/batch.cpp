@@ -18,11 +18,9 @@ Status cuda_fail(const char* what, cudaError_t e) {
     if (_e != cudaSuccess) return cuda_fail(#call, _e); \
   } while (0)
 
-size_t resident_bytes(int W, int H, unsigned long long lut_entries) {
+size_t resident_bytes(int W, int H, const LutShape& lut) {
   size_t b = (size_t)(((W + 3) & ~3) + 8) * (size_t)(H + 2);
-  b = (b + 15) & ~(size_t)15;
-  if (lut_entries && lut_entries <= kLutSmemMaxEntries) b += (size_t)lut_entries * 2;
-  return b;
+  return ((b + 15) & ~(size_t)15) + lut_smem_bytes(lut);
 }
 }  // namespace
 
@@ -71,7 +69,7 @@ Status Batch::create(std::shared_ptr<Ruleset> r, int count, const int* widths, c
   SE_CUDA(cudaMemsetAsync(arena, 0, bytes, stream));
   desc.resize((size_t)n);
   const size_t maxsm = rs->module->max_dyn_smem;
-  const unsigned long long lut = rs->cuda.lut_entries;
+  const LutShape lut = rs->lut_shape();
   // size classes for whole-world CTAs: occupancy is set by the largest world of a class
   const size_t class_max[3] = {40 * 1024, 100 * 1024, maxsm};
   const int class_threads[3] = {256, 512, 1024};
@@ -184,7 +182,7 @@ Status Batch::launch_body(int F, cudaStream_t s) {
                              dim3((unsigned)R.threads), args, R.smem, side[c]));
     SE_CUDA(cudaEventRecord(join[c], side[c]));
   }
-  const size_t smem = tile_smem_bytes(*variant, rs->cuda.lut_entries);
+  const size_t smem = tile_smem_bytes(*variant, rs->lut_shape());
   for (int p = 0; p < P; ++p) {
     int pass = p, done = p * k, kp = std::min(k, F - p * k);
     const WorldDesc* dd = d_desc;
@@ -221,7 +219,7 @@ Status Batch::autotune(int reps, int* best_k) {
     for (const TileVariant& v : tile_variants()) {
       Status s = set_variant(&v);
       if (!s.ok()) return s;
-      const size_t smem = tile_smem_bytes(v, rs->cuda.lut_entries);
+      const size_t smem = tile_smem_bytes(v, rs->lut_shape());
       const uint16_t* lut = rs->d_lut;
       const WorldDesc* dd = d_desc;
       const TileJob* jb = d_jobs;
@@ -314,7 +312,7 @@ Status Batch::step_plain(int F) {
       v1 = &t;
       break;
     }
-  const size_t smem = tile_smem_bytes(*v1, rs->cuda.lut_entries);
+  const size_t smem = tile_smem_bytes(*v1, rs->lut_shape());
   cudaKernel_t kern = rs->module->get(v1->name());
   const uint16_t* lut = rs->d_lut;
   for (int f = 0; f < F; ++f) {

@@ -35,13 +35,16 @@ Status Ruleset::ensure_loaded() {
   if (module) return Status::Ok();
   auto m = std::make_unique<Module>();
   std::string err;
-  if (!m->load(cubin, cuda.lut_entries, &err)) return {SE_ERR_CUDA, err};
+  if (!m->load(cubin, lut_shape(), &err)) return {SE_ERR_CUDA, err};
   if (cuda.lut_entries) {  // build the block transition table with the rules themselves
-    cudaError_t e = cudaMalloc(&d_lut, (size_t)cuda.lut_entries * sizeof(uint16_t));
+    const size_t table = ((size_t)cuda.lut_entries * sizeof(uint16_t) + 15) & ~(size_t)15;
+    cudaError_t e = cudaMalloc(&d_lut, table + (size_t)cuda.lut_static_words * 4);
     if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
     void* args[] = {(void*)&d_lut};
     const unsigned blocks = (unsigned)std::min<unsigned long long>((cuda.lut_entries + 255) / 256, 4096);
     SE_CUDA(cudaLaunchKernel((const void*)m->get("se_build_lut"), dim3(blocks), dim3(256), args, 0, nullptr));
+    const unsigned sblocks = (unsigned)((cuda.lut_static_words + 255) / 256);
+    SE_CUDA(cudaLaunchKernel((const void*)m->get("se_build_static"), dim3(sblocks), dim3(256), args, 0, nullptr));
     SE_CUDA(cudaDeviceSynchronize());
   }
   module = std::move(m);
@@ -146,7 +149,7 @@ Status World::launch_tiles(int f0, int k, const TileVariant* v, bool commit) {
   const uint16_t* lut = rs->d_lut;
   void* args[] = {(void*)&src, (void*)&dst, &Wv, &Hv, &f0, &k, (void*)&lut};
   dim3 grid((unsigned)((W + v->tw - 1) / v->tw), (unsigned)((H + v->th - 1) / v->th));
-  const size_t smem = tile_smem_bytes(*v, rs->cuda.lut_entries);
+  const size_t smem = tile_smem_bytes(*v, rs->lut_shape());
   Timed* t = nullptr;
   if (timing) {
     if (timed_used == timed.size()) {

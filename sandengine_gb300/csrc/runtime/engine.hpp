@@ -33,8 +33,11 @@ struct Ruleset {
   bool compiled = false;
   std::mutex mu;
   std::unique_ptr<Module> module;  // loaded on first use on a device
-  uint16_t* d_lut = nullptr;       // block transition table (when cuda.lut_entries > 0)
+  // Block transition table (when cuda.lut_entries > 0), followed 16-byte aligned by the
+  // bitset of static keys.
+  uint16_t* d_lut = nullptr;
   ~Ruleset();
+  LutShape lut_shape() const { return {cuda.lut_entries, cuda.lut_static_words}; }
   int num_materials() const { return (int)parsed.materials.size(); }
   Status compile();
   Status ensure_loaded();

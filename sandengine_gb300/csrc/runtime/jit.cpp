@@ -155,13 +155,20 @@ Module::~Module() {
   if (lib) cudaLibraryUnload(lib);
 }
 
-size_t tile_smem_bytes(const TileVariant& t, unsigned long long lut_entries) {
-  size_t b = (t.smem_bytes() + 15) & ~(size_t)15;
-  if (lut_entries && lut_entries <= kLutSmemMaxEntries) b += (size_t)lut_entries * 2;
+size_t lut_smem_bytes(const LutShape& lut) {
+  if (lut.entries && lut.entries <= kLutSmemMaxEntries) return ((size_t)lut.entries * 2 + 15) & ~(size_t)15;
+  return 0;
+}
+
+size_t tile_smem_bytes(const TileVariant& t, const LutShape& lut) {
+  size_t b = ((t.smem_bytes() + 15) & ~(size_t)15) + lut_smem_bytes(lut);
+  // with a table: 48-byte header (slack, list counters, uniform-material flags), then the
+  // per-step list of chunks (4 blocks) to evaluate, one u16 offset each
+  if (lut.entries) b += 48 + ((2 * (size_t)(t.sw() / 8) * (size_t)(t.sh() / 2) + 15) & ~(size_t)15);
   return b;
 }
 
-bool Module::load(const std::string& cubin, unsigned long long lut_entries, std::string* err) {
+bool Module::load(const std::string& cubin, const LutShape& lut, std::string* err) {
   cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e != cudaSuccess) {
     *err = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
@@ -169,7 +176,10 @@ bool Module::load(const std::string& cubin, unsigned long long lut_entries, std:
     return false;
   }
   std::vector<std::string> names = {"se_edit", "se_resident", "se_batch_finalize"};
-  if (lut_entries) names.push_back("se_build_lut");
+  if (lut.entries) {
+    names.push_back("se_build_lut");
+    names.push_back("se_build_static");
+  }
   for (auto& t : tile_variants()) {
     names.push_back(t.name());
     names.push_back(t.multi_name());
@@ -187,7 +197,7 @@ bool Module::load(const std::string& cubin, unsigned long long lut_entries, std:
   for (auto& t : tile_variants()) {
     for (const std::string& n : {t.name(), t.multi_name(), t.serve_name()}) {
       e = cudaFuncSetAttribute((const void*)kernels[n], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)tile_smem_bytes(t, lut_entries));
+                               (int)tile_smem_bytes(t, lut));
       if (e != cudaSuccess) {
         *err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
         return false;

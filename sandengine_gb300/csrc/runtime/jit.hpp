@@ -18,7 +18,9 @@ struct TileVariant {
   std::string serve_name() const;  // serving iteration kernel (per-world frame counts)
   int halo_x() const { return ((kmax + 3) / 4) * 4; }
   int halo_y() const { return kmax; }
-  size_t smem_bytes() const { return (size_t)(tw + 2 * halo_x()) * (size_t)(th + 2 * halo_y()); }
+  int sw() const { return tw + 2 * halo_x(); }  // shared array: tile plus halo
+  int sh() const { return th + 2 * halo_y(); }
+  size_t smem_bytes() const { return (size_t)sw() * (size_t)sh(); }
 };
 const std::vector<TileVariant>& tile_variants();
 
@@ -26,8 +28,17 @@ const std::vector<TileVariant>& tile_variants();
 // CTA (SE_LUT_SMEM_MAX_ENTRIES in kernels/margolus.cuh); larger ones are read from global
 // memory through the read-only cache.
 constexpr unsigned long long kLutSmemMaxEntries = 16384;
-// Dynamic shared memory of a tile launch: the u8 tile, then the table when it fits.
-size_t tile_smem_bytes(const TileVariant& t, unsigned long long lut_entries);
+// Size of a rule set's block transition table: its u16 entries and the 32-bit words of the
+// bitset of static keys that follows it (both 0 without a table).
+struct LutShape {
+  unsigned long long entries = 0, static_words = 0;
+};
+// Shared memory the table copy of a CTA takes (the table when it fits, rounded up to 16
+// bytes).  The static-key bitset stays in global memory.
+size_t lut_smem_bytes(const LutShape& lut);
+// Dynamic shared memory of a tile launch: the u8 tile, then the table copy, then (with a
+// table) the per-step list of chunks to evaluate.
+size_t tile_smem_bytes(const TileVariant& t, const LutShape& lut);
 
 // Full device source: prelude + generated rules + kernel template + instantiations.
 std::string kernel_source(const std::string& generated_rules);
@@ -40,7 +51,7 @@ struct Module {
   std::map<std::string, cudaKernel_t> kernels;
   size_t max_dyn_smem = 0;  // opt-in dynamic shared memory per CTA on this device
   ~Module();
-  bool load(const std::string& cubin, unsigned long long lut_entries, std::string* err);
+  bool load(const std::string& cubin, const LutShape& lut, std::string* err);
   cudaKernel_t get(const std::string& name) const;
 };
 

@@ -248,7 +248,7 @@ Status Server::run_batched() {
   iter_events.push_back(t0);  // index 0: the time origin
   const Clock::time_point host_t0 = Clock::now();
   const int K = variant->kmax;
-  const size_t smem = tile_smem_bytes(*variant, rs->cuda.lut_entries);
+  const size_t smem = tile_smem_bytes(*variant, rs->lut_shape());
   cudaKernel_t kern = rs->module->get(variant->serve_name());
   const uint16_t* lut = rs->d_lut;
   size_t next = 0;
@@ -392,7 +392,7 @@ Status Server::run_plain() {
       v1 = &t;
       break;
     }
-  const size_t smem = tile_smem_bytes(*v1, rs->cuda.lut_entries);
+  const size_t smem = tile_smem_bytes(*v1, rs->lut_shape());
   cudaKernel_t kern = rs->module->get(v1->name());
   const uint16_t* lut = rs->d_lut;
   cudaEvent_t t0;

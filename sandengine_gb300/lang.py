@@ -70,6 +70,21 @@ class Ruleset:
         check(lib().se_ruleset_material_id(self._h, name.encode(), ctypes.byref(i)))
         return i.value
 
+    def table(self):
+        """(table, static_bits) as built on the current CUDA device: the block transition
+        table (u16 entries) and the bitset of static keys (u32 words), or (None, None) when
+        the rules take the direct path.  Needs a GPU."""
+        import numpy as np
+        e, w = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        check(lib().se_ruleset_table(self._h, None, 0, None, 0, ctypes.byref(e), ctypes.byref(w)))
+        if not e.value:
+            return None, None
+        t = np.empty(e.value, dtype=np.uint16)
+        b = np.empty(w.value, dtype=np.uint32)
+        check(lib().se_ruleset_table(self._h, t.ctypes.data, t.size, b.ctypes.data, b.size, ctypes.byref(e),
+                                     ctypes.byref(w)))
+        return t, b
+
     def compile(self) -> None:
         """NVRTC-compile the kernels for sm_103a (needs no GPU; cached on disk)."""
         check(lib().se_ruleset_compile(self._h))

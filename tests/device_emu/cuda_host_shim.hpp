@@ -24,6 +24,10 @@ inline void __syncthreads() {}
 struct uint4 {
   unsigned x, y, z, w;
 };
+struct uint2 {
+  unsigned x, y;
+};
+inline uint2 make_uint2(unsigned a, unsigned b) { return uint2{a, b}; }
 struct int4 {
   int x, y, z, w;
 };
@@ -42,4 +46,27 @@ inline float __uint_as_float(unsigned u) {
   float f;
   __builtin_memcpy(&f, &u, 4);
   return f;
+}
+inline unsigned __funnelshift_r(unsigned lo, unsigned hi, unsigned s) {
+  const unsigned long long v = ((unsigned long long)hi << 32) | lo;
+  return (unsigned)(v >> (s & 31));
+}
+inline unsigned __byte_perm(unsigned x, unsigned y, unsigned s) {
+  const unsigned long long v = ((unsigned long long)y << 32) | x;
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) {
+    const unsigned sel = (s >> (4 * i)) & 7u;
+    r |= (unsigned)((v >> (8 * sel)) & 0xffu) << (8 * i);
+  }
+  return r;
+}
+// Warp operations for a warp of one thread (lane 0).
+inline unsigned __ballot_sync(unsigned, bool p) { return p ? 1u : 0u; }
+template <class T>
+inline T __shfl_sync(unsigned, T v, int) { return v; }
+inline int __popc(unsigned v) { return __builtin_popcount(v); }
+inline int atomicAdd(int* p, int v) {
+  const int old = *p;
+  *p = old + v;
+  return old;
 }

@@ -21,11 +21,28 @@ VARIANTS = [(128, 64, 1), (256, 32, 1), (128, 32, 1), (128, 64, 2), (128, 64, 4)
 DRIVER = r'''
 alignas(16) uint8_t se_smem[1 << 21];
 static uint16_t* g_lut = nullptr;
+extern "C" const uint16_t* emu_lut() { return g_lut; }
+extern "C" const uint32_t* emu_static() {
+#ifdef SE_LUT
+  return reinterpret_cast<const uint32_t*>(reinterpret_cast<const uint8_t*>(g_lut) + SE_LUT_STATIC_OFF);
+#else
+  return nullptr;
+#endif
+}
+extern "C" unsigned emu_static_words() {
+#ifdef SE_LUT
+  return SE_LUT_STATIC_WORDS;
+#else
+  return 0;
+#endif
+}
 extern "C" int emu_build_lut() {
 #ifdef SE_LUT
-  g_lut = new uint16_t[SE_LUT_ENTRIES];
+  g_lut = reinterpret_cast<uint16_t*>(new uint32_t[(SE_LUT_STATIC_OFF + 4u * SE_LUT_STATIC_WORDS) / 4u]);
   blockDim.x = 1; gridDim.x = 1; threadIdx.x = 0; blockIdx.x = 0;
   se_build_lut(g_lut);
+  for (unsigned w = 0; w < SE_LUT_STATIC_WORDS; ++w) { blockIdx.x = w; se_build_static(g_lut); }
+  blockIdx.x = 0;
   return 1;
 #else
   return 0;

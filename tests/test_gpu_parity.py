@@ -156,3 +156,22 @@ def test_digest_and_histogram_on_device(se, rulesets):
     hist = sim.histogram(7)
     ref = np.bincount(np.minimum(g.ravel(), 6), minlength=7)
     assert np.array_equal(hist, ref)
+
+
+@pytest.mark.parametrize("name", ["four_materials", "twelve_materials"])
+def test_device_table_matches_emulated_rules(se, rulesets, name):
+    """The block transition table and static-key bitset built on the GPU (se_build_lut,
+    se_build_static) equal those the same device code builds on the CPU."""
+    import ctypes
+    from tests.device_emu.emu import Emu
+    rs = se.parse_string(rulesets[name])
+    table, bits = rs.table()
+    assert table is not None
+    E = Emu(rs, lut=True)
+    E.lib.emu_lut.restype = ctypes.POINTER(ctypes.c_uint16)
+    E.lib.emu_static.restype = ctypes.POINTER(ctypes.c_uint32)
+    want_t = np.ctypeslib.as_array(E.lib.emu_lut(), shape=(table.size,))
+    want_b = np.ctypeslib.as_array(E.lib.emu_static(), shape=(bits.size,))
+    assert np.array_equal(table, want_t)
+    assert np.array_equal(bits, want_b)
+    assert 0 < int(np.unpackbits(bits.view(np.uint8)).sum()) < 32 * bits.size

@@ -86,3 +86,34 @@ def test_edit_pass_matches_port(emus, ports, name):
         b = E.tiles(b, f, 1)
         E.edit(b, mods)
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["four_materials", "twelve_materials"])
+def test_static_key_bitset(se, rulesets, name):
+    """Bit `key` of se_build_static's bitset is set exactly when every table entry of that
+    key maps the block to itself; the all-EMPTY key is always static."""
+    import ctypes
+    rs = se.parse_string(rulesets[name])
+    E = Emu(rs, lut=True)
+    assert E.has_lut
+    src = rs.kernel_source
+    bits = int(src.split("#define SE_LUT_BITS ")[1].split()[0])
+    entries = int(src.split("#define SE_LUT_ENTRIES ")[1].split("u")[0])
+    keys = 1 << (4 * bits)
+    E.lib.emu_lut.restype = ctypes.POINTER(ctypes.c_uint16)
+    E.lib.emu_static.restype = ctypes.POINTER(ctypes.c_uint32)
+    E.lib.emu_static_words.restype = ctypes.c_uint
+    words = E.lib.emu_static_words()
+    assert words == max(1, keys // 32)
+    st = np.ctypeslib.as_array(E.lib.emu_static(), shape=(words,)).copy()
+    C = entries // keys
+    lut = np.ctypeslib.as_array(E.lib.emu_lut(), shape=(entries,)).reshape(keys, C).astype(np.uint32)
+    m = (1 << bits) - 1
+    k = np.arange(keys, dtype=np.uint32)
+    a, b, c, d = k & m, (k >> bits) & m, (k >> (2 * bits)) & m, (k >> (3 * bits)) & m
+    self_ = a | (b << 4) | (c << 8) | (d << 12)
+    want = np.all(lut == self_[:, None], axis=1)
+    got = ((st[k >> 5] >> (k & 31)) & 1).astype(bool)
+    assert np.array_equal(got, want)
+    assert got[0]
+    assert 0 < got.sum() < keys
