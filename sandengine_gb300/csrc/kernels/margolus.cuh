@@ -242,9 +242,8 @@ __device__ __forceinline__ void se_st8(uint8_t* p, uint32_t lo, uint32_t hi) {
   }
 }
 
-// Table lookup for a block given as the 4 bytes [a, b, c, d] (ids < 16) with hash base x;
-// returns the new block in the same layout.
-__device__ __forceinline__ uint32_t se_lut_word(uint32_t abcd, uint32_t x, const uint16_t* __restrict__ lut) {
+// Table index of a block given as the 4 bytes [a, b, c, d] (ids < 16) with hash base x.
+__device__ __forceinline__ uint32_t se_lut_word_index(uint32_t abcd, uint32_t x) {
 #if SE_LUT_BITS == 4
   const uint32_t y = abcd | (abcd >> 4);  // byte 0 = a | b << 4, byte 2 = c | d << 4
   const uint32_t key = (y & 0xffu) | ((y >> 8) & 0xff00u);
@@ -252,13 +251,18 @@ __device__ __forceinline__ uint32_t se_lut_word(uint32_t abcd, uint32_t x, const
   const uint32_t key = se_gen::lut_key(abcd & 0xffu, (abcd >> 8) & 0xffu, (abcd >> 16) & 0xffu, abcd >> 24);
 #endif
   const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u), h3 = se_mix(x * 213132u);
-  const uint32_t idx = se_gen::lut_index_key(key, h0, h1, h2, h3);
+  return se_gen::lut_index_key(key, h0, h1, h2, h3);
+}
+__device__ __forceinline__ uint32_t se_lut_fetch(const uint16_t* __restrict__ lut, uint32_t idx) {
 #if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
-  const uint32_t o = lut[idx];
+  return lut[idx];
 #else
-  const uint32_t o = __ldg(lut + idx);
+  return __ldg(lut + idx);
 #endif
-  const uint32_t t = (o & 0xffu) | ((o << 8) & 0xff0000u);  // nibbles a b c d -> bytes
+}
+// A table entry (nibbles a | b << 4 | c << 8 | d << 12) as the 4 bytes [a, b, c, d].
+__device__ __forceinline__ uint32_t se_lut_bytes(uint32_t o) {
+  const uint32_t t = (o & 0xffu) | ((o << 8) & 0xff0000u);
   return (t | (t << 4)) & 0x0f0f0f0fu;
 }
 
@@ -325,12 +329,16 @@ __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __
     se_ld8<OX>(p, a0, a1);
     se_ld8<OX>(p + SW, b0, b1);
     const uint32_t x = (uint32_t)(gx0 + lx) * 461u + (uint32_t)(gy0 + ly) * 2131u + xf;
-    uint32_t B0 = __byte_perm(a0, b0, 0x5410), B1 = __byte_perm(a0, b0, 0x7632);  // [a, b, c, d] per block
-    uint32_t B2 = __byte_perm(a1, b1, 0x5410), B3 = __byte_perm(a1, b1, 0x7632);
-    if (B0) B0 = se_lut_word(B0, x, lut);  // next block: origin x + 2
-    if (B1) B1 = se_lut_word(B1, x + 922u, lut);
-    if (B2) B2 = se_lut_word(B2, x + 1844u, lut);
-    if (B3) B3 = se_lut_word(B3, x + 2766u, lut);
+    // [a, b, c, d] of the four blocks; block origins are 2 cells apart (x + 922 each).  No
+    // branch on all-EMPTY blocks (the table maps them to themselves), so the four lookups
+    // are in flight together.
+    const uint32_t i0 = se_lut_word_index(__byte_perm(a0, b0, 0x5410), x);
+    const uint32_t i1 = se_lut_word_index(__byte_perm(a0, b0, 0x7632), x + 922u);
+    const uint32_t i2 = se_lut_word_index(__byte_perm(a1, b1, 0x5410), x + 1844u);
+    const uint32_t i3 = se_lut_word_index(__byte_perm(a1, b1, 0x7632), x + 2766u);
+    const uint32_t o0 = se_lut_fetch(lut, i0), o1 = se_lut_fetch(lut, i1), o2 = se_lut_fetch(lut, i2),
+                   o3 = se_lut_fetch(lut, i3);
+    const uint32_t B0 = se_lut_bytes(o0), B1 = se_lut_bytes(o1), B2 = se_lut_bytes(o2), B3 = se_lut_bytes(o3);
     se_st8<OX>(p, __byte_perm(B0, B1, 0x5410), __byte_perm(B2, B3, 0x5410));
     se_st8<OX>(p + SW, __byte_perm(B0, B1, 0x7632), __byte_perm(B2, B3, 0x7632));
   }
