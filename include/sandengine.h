@@ -107,6 +107,25 @@ void se_ruleset_free(se_ruleset* rs);
  * counter 0 on the current CUDA device.  Compiles the rule set if needed. */
 int se_world_create(se_ruleset* rs, int width, int height, se_world** out);
 void se_world_destroy(se_world* w);
+
+/* ---- row bands of one world (no counterpart in the reference, which runs one world on
+ * one GPU) ------------------------------------------------------------------------------
+ * A band world holds rows [row0, row0 + rows) of a width x world_height world plus up to
+ * `halo` rows on either side (clipped to the world).  It steps like a world in world
+ * coordinates (hash, block parity, WALL border, edit positions), but may advance at most
+ * `halo` frames per se_world_step: after n frames its rows at least n rows inside the
+ * buffer are exact (its own rows, when n <= halo), and the halo rows must be refreshed from
+ * the neighbouring bands (se_world_copy_rows) before the next step.  se_world_set_grid /
+ * get_grid / digest / histogram cover the whole buffer; snapshots refuse bands. */
+int se_world_create_band(se_ruleset* rs, int width, int world_height, int row0, int rows, int halo,
+                         se_world** out);
+/* Buffer rows [*buffer_row0, *buffer_row0 + *buffer_rows) of a *world_height-row world;
+ * *halo = -1 for a whole world. */
+int se_world_band_info(const se_world* w, int* buffer_row0, int* buffer_rows, int* world_height, int* halo);
+/* Copies world rows [row, row + nrows) (inside the buffer) of the current grid to `ptr`
+ * (to_world = 0) or from `ptr` into the grid (to_world = 1).  `ptr` is host or device
+ * memory (the copy direction is inferred from it); returns when the copy is done. */
+int se_world_copy_rows(se_world* w, int row, int nrows, void* ptr, int to_world);
 /* Work is issued on this stream (cudaStream_t; NULL = the world's own stream). */
 int se_world_set_stream(se_world* w, void* cuda_stream);
 int se_world_get_stream(se_world* w, void** cuda_stream);

@@ -57,6 +57,9 @@ _SIGS = {
     "se_ruleset_compile": ([_P], _I),
     "se_ruleset_num_materials": ([_P, ctypes.POINTER(_I)], _I),
     "se_ruleset_material_id": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
+    "se_world_create_band": ([_P, _I, _I, _I, _I, _I, ctypes.POINTER(_P)], _I),
+    "se_world_band_info": ([_P] + [ctypes.POINTER(_I)] * 4, _I),
+    "se_world_copy_rows": ([_P, _I, _I, _P, _I], _I),
     "se_ruleset_table": ([_P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_ulonglong),
                           ctypes.POINTER(ctypes.c_ulonglong)], _I),
     "se_ruleset_free": ([_P], None),

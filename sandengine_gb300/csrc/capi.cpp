@@ -175,6 +175,49 @@ SE_API int se_ruleset_material_id(const se_ruleset* rs, const char* name, int* i
 
 SE_API void se_ruleset_free(se_ruleset* rs) { delete rs; }
 
+SE_API int se_world_create_band(se_ruleset* rs, int width, int world_height, int row0, int rows, int halo,
+                                se_world** out) {
+  return guard([&] {
+    if (!rs || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    auto w = std::make_unique<se::rt::World>();
+    se::rt::Status s = w->create_band(rs->rs, width, world_height, row0, rows, halo);
+    if (!s.ok()) return ret(s);
+    *out = new se_world{std::move(w)};
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_band_info(const se_world* w, int* buffer_row0, int* buffer_rows, int* world_height,
+                              int* halo) {
+  return guard([&] {
+    if (!w || !buffer_row0 || !buffer_rows || !world_height || !halo)
+      return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    *buffer_row0 = w->w->ya;
+    *buffer_rows = w->w->H;
+    *world_height = w->w->wh;
+    *halo = w->w->halo;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_copy_rows(se_world* w, int row, int nrows, void* ptr, int to_world) {
+  return guard([&] {
+    if (!w || !ptr || nrows < 0) return fail(SE_ERR_INVALID_ARGUMENT, "bad argument");
+    auto& W = *w->w;
+    if (row < W.ya || (int64_t)row + nrows > (int64_t)W.ya + W.H)
+      return fail(SE_ERR_INVALID_ARGUMENT, "rows outside the world's buffer");
+    if (nrows == 0) return (int)SE_OK;
+    uint32_t* g = W.buf[W.cur] + (size_t)(row - W.ya) * W.W;
+    const size_t bytes = (size_t)nrows * W.W * sizeof(uint32_t);
+    cudaError_t e = to_world ? cudaMemcpyAsync(g, ptr, bytes, cudaMemcpyDefault, W.stream)
+                             : cudaMemcpyAsync(ptr, g, bytes, cudaMemcpyDefault, W.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(W.stream);
+    if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    return (int)SE_OK;
+  });
+}
+
 SE_API int se_world_create(se_ruleset* rs, int width, int height, se_world** out) {
   return guard([&] {
     if (!rs || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
@@ -585,6 +628,7 @@ SE_API int se_world_save(se_world* w, const char* path) {
   return guard([&] {
     if (!w || !path) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
     auto& W = *w->w;
+    if (W.halo >= 0) return fail(SE_ERR_INVALID_ARGUMENT, "snapshots hold whole worlds, not bands");
     std::vector<uint32_t> cells((size_t)W.W * W.H);
     int rc = grid_copy(w, cells.data(), cells.size(), false, true);
     if (rc) return rc;
@@ -599,6 +643,7 @@ SE_API int se_world_load(se_world* w, const char* path) {
   return guard([&] {
     if (!w || !path) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
     auto& W = *w->w;
+    if (W.halo >= 0) return fail(SE_ERR_INVALID_ARGUMENT, "snapshots hold whole worlds, not bands");
     se::rt::SnapshotHeader h;
     std::vector<uint32_t> cells;
     std::string err;

@@ -454,9 +454,15 @@ __device__ __forceinline__ void se_store_region(const uint8_t* sm, int SW, int h
 
 // Advances the tile with top-left cell (X0, Y0) of a W x H world by k <= KMAX frames whose
 // counters are f0, f0+1, ... (all >= 2; the host handles the frame-1 clear).
+// src and dst hold the world rows [ya, yb) (row gy at (gy - ya) * W): the whole world, or a
+// band of it with its halo.  Rows outside the buffer read as WALL, like those outside the
+// world; inside the world that is wrong, but a wrong cell can only spread one row per
+// frame, so after n frames every row at least n rows inside the buffer is exact.  Hashes,
+// block parities and the world border use world coordinates.
 template <int TW, int TH, int KMAX, int NT>
 __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W,
-                                            int H, int f0, int k, const uint16_t* __restrict__ lut, int X0, int Y0) {
+                                            int H, int f0, int k, const uint16_t* __restrict__ lut, int X0, int Y0,
+                                            int ya, int yb) {
   constexpr int HX = ((KMAX + 3) / 4) * 4, HY = KMAX;
   constexpr int SW = TW + 2 * HX, SH = TH + 2 * HY, WPR = SW / 4;
   static_assert(TW % 4 == 0, "tile width must be a multiple of 4");
@@ -480,16 +486,16 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
     const int r = i / WPR, c = i - r * WPR;
     const int gy = gy0 + r, gx = gx0 + 4 * c;
     uint32_t packed;
-    if (gy < 0 || gy >= H) {
+    if (gy < ya || gy >= yb) {
       packed = 0x02020202u;
     } else if (vec && gx >= 0 && gx + 3 < W) {
-      const uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (size_t)gy * W + gx));
+      const uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (size_t)(gy - ya) * W + gx));
       packed = se_norm(v.x) | (se_norm(v.y) << 8) | (se_norm(v.z) << 16) | (se_norm(v.w) << 24);
     } else {
       packed = 0;
       for (int e = 0; e < 4; ++e) {
         const int x = gx + e;
-        const uint32_t id = (x >= 0 && x < W) ? se_norm(__ldg(src + (size_t)gy * W + x)) : SE_WALL;
+        const uint32_t id = (x >= 0 && x < W) ? se_norm(__ldg(src + (size_t)(gy - ya) * W + x)) : SE_WALL;
         packed |= id << (8 * e);
       }
     }
@@ -533,23 +539,26 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   for (int i = threadIdx.x; i < OWPR * TH; i += NT) {
     const int r = i / OWPR, c = i - r * OWPR;
     const int gy = Y0 + r, gx = X0 + 4 * c;
-    if (gy >= H || gx >= W) continue;
+    if (gy >= yb || gx >= W) continue;
     const uint32_t packed = *reinterpret_cast<const uint32_t*>(sm + (r + HY) * SW + HX + 4 * c);
+    uint32_t* out = dst + (size_t)(gy - ya) * W;
     if (vec && gx + 3 < W) {
       const uint4 v = make_uint4(packed & 0xffu, (packed >> 8) & 0xffu, (packed >> 16) & 0xffu, packed >> 24);
-      *reinterpret_cast<uint4*>(dst + (size_t)gy * W + gx) = v;
+      *reinterpret_cast<uint4*>(out + gx) = v;
     } else {
       for (int e = 0; e < 4; ++e)
-        if (gx + e < W) dst[(size_t)gy * W + gx + e] = (packed >> (8 * e)) & 0xffu;
+        if (gx + e < W) out[gx + e] = (packed >> (8 * e)) & 0xffu;
     }
   }
 }
 
-// Single world: the tile is (blockIdx.x, blockIdx.y).
+// One world, or the band of world rows [ya, yb) held by src and dst: the tile is
+// (blockIdx.x, blockIdx.y) counted from row ya.
 template <int TW, int TH, int KMAX, int NT>
 __device__ __forceinline__ void se_tile_impl(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W,
-                                             int H, int f0, int k, const uint16_t* __restrict__ lut) {
-  se_tile_run<TW, TH, KMAX, NT>(src, dst, W, H, f0, k, lut, blockIdx.x * TW, blockIdx.y * TH);
+                                             int H, int f0, int k, const uint16_t* __restrict__ lut, int ya, int yb) {
+  if (ya < 0 || yb > H || ya >= yb || k < 1 || k > KMAX) return;  // the host validates these too
+  se_tile_run<TW, TH, KMAX, NT>(src, dst, W, H, f0, k, lut, blockIdx.x * TW, ya + blockIdx.y * TH, ya, yb);
 }
 
 // ---- many worlds -------------------------------------------------------------------------
@@ -580,7 +589,7 @@ __device__ __forceinline__ void se_mtile_impl(const SeWorldDesc* __restrict__ wo
   const int in = w.cur ^ (pass & 1);
   const uint32_t* src = in ? w.buf1 : w.buf0;
   uint32_t* dst = in ? w.buf0 : w.buf1;
-  se_tile_run<TW, TH, KMAX, NT>(src, dst, w.W, w.H, w.frame + 1 + frames_done, k, lut, job.x0, job.y0);
+  se_tile_run<TW, TH, KMAX, NT>(src, dst, w.W, w.H, w.frame + 1 + frames_done, k, lut, job.x0, job.y0, 0, w.H);
 }
 
 // One serving iteration: descs[a] is the a-th active world, with its frames for this
@@ -602,7 +611,7 @@ __device__ __forceinline__ void se_stile_impl(const SeWorldDesc* __restrict__ de
   const int ty = local / tiles_x, tx = local - ty * tiles_x;
   const uint32_t* src = w.cur ? w.buf1 : w.buf0;
   uint32_t* dst = w.cur ? w.buf0 : w.buf1;
-  se_tile_run<TW, TH, KMAX, NT>(src, dst, w.W, w.H, w.frame + 1, w.pad0, lut, tx * TW, ty * TH);
+  se_tile_run<TW, TH, KMAX, NT>(src, dst, w.W, w.H, w.frame + 1, w.pad0, lut, tx * TW, ty * TH, 0, w.H);
 }
 
 // Whole-world launch: CTA b holds world ids[b] entirely in shared memory (plus a WALL
@@ -673,8 +682,9 @@ struct SeEditParams {
   long long starts[257];
 };
 
+// grid holds world rows from row0 on (the boxes lie within them).
 extern "C" __global__ void __launch_bounds__(256) se_edit(uint32_t* __restrict__ grid, int W, int H, int nmods,
-                                                          long long total, const SeEditParams p) {
+                                                          long long total, const SeEditParams p, int row0) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
   int lo = 0, hi = nmods - 1;  // last q with starts[q] <= t
@@ -692,5 +702,5 @@ extern "C" __global__ void __launch_bounds__(256) se_edit(uint32_t* __restrict__
   for (int r = q + 1; r < nmods; ++r)
     if (se_mod_hits(p.mods[r], x, y)) return;
   if (p.mods[q].mat == (int)SE_NULL) return;
-  grid[(size_t)y * W + x] = (uint32_t)p.mods[q].mat;
+  grid[(size_t)(y - row0) * W + x] = (uint32_t)p.mods[q].mat;
 }

@@ -312,9 +312,6 @@ Status Batch::step_plain(int F) {
       v1 = &t;
       break;
     }
-  const size_t smem = tile_smem_bytes(*v1, rs->lut_shape());
-  cudaKernel_t kern = rs->module->get(v1->name());
-  const uint16_t* lut = rs->d_lut;
   for (int f = 0; f < F; ++f) {
     for (auto& d : desc) {
       const int fr = d.frame + 1;
@@ -323,10 +320,8 @@ Status Batch::step_plain(int F) {
       } else {
         const uint32_t* src = d.cur ? d.buf1 : d.buf0;
         uint32_t* dst = d.cur ? d.buf0 : d.buf1;
-        int W = d.W, H = d.H, f0 = fr, k = 1;
-        void* args[] = {(void*)&src, (void*)&dst, &W, &H, &f0, &k, (void*)&lut};
-        dim3 grid((unsigned)((W + v1->tw - 1) / v1->tw), (unsigned)((H + v1->th - 1) / v1->th));
-        SE_CUDA(cudaLaunchKernel((const void*)kern, grid, dim3((unsigned)v1->nt), args, smem, stream));
+        Status s = launch_tile_kernel(*rs, *v1, src, dst, d.W, d.H, fr, 1, 0, d.H, stream);
+        if (!s.ok()) return s;
         d.cur ^= 1;
       }
       d.frame = fr;

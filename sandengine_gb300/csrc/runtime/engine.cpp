@@ -72,6 +72,7 @@ Status World::create(std::shared_ptr<Ruleset> r, int w, int h) {
   rs = std::move(r);
   W = w;
   H = h;
+  if (wh == 0) wh = h;
   Status s = rs->ensure_loaded();
   if (!s.ok()) return s;
   SE_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
@@ -88,6 +89,16 @@ Status World::create(std::shared_ptr<Ruleset> r, int w, int h) {
   SE_CUDA(cudaMemsetAsync(buf[0], 0, bytes, stream));  // Simulation::new: all-zero textures
   SE_CUDA(cudaStreamSynchronize(stream));
   return Status::Ok();
+}
+
+Status World::create_band(std::shared_ptr<Ruleset> r, int w, int world_h, int row0, int rows, int hal) {
+  if (w <= 0 || world_h <= 0 || rows <= 0 || row0 < 0 || (int64_t)row0 + rows > world_h || hal < 0)
+    return {SE_ERR_INVALID_ARGUMENT, "band rows must lie within the world and the halo be >= 0"};
+  const int a = std::max(0, row0 - hal), b = (int)std::min<int64_t>(world_h, (int64_t)row0 + rows + hal);
+  wh = world_h;
+  ya = a;
+  halo = hal;
+  return create(std::move(r), w, b - a);
 }
 
 int World::default_k() const {
@@ -140,16 +151,21 @@ Status World::autotune(int reps, int* best_k) {
   return Status::Ok();
 }
 
+Status launch_tile_kernel(const Ruleset& rs, const TileVariant& v, const uint32_t* src, uint32_t* dst, int W, int H,
+                          int f0, int k, int ya, int yb, cudaStream_t stream) {
+  if (v.kmax < k || k < 1) return {SE_ERR_INVALID_ARGUMENT, "no kernel variant for this many frames per launch"};
+  if (ya < 0 || yb > H || ya >= yb) return {SE_ERR_INVALID_ARGUMENT, "tile rows outside the world"};
+  cudaKernel_t kern = rs.module->get(v.name());
+  const uint16_t* lut = rs.d_lut;
+  void* args[] = {(void*)&src, (void*)&dst, &W, &H, &f0, &k, (void*)&lut, &ya, &yb};  // se_tile_impl's order
+  dim3 grid((unsigned)((W + v.tw - 1) / v.tw), (unsigned)((yb - ya + v.th - 1) / v.th));
+  SE_CUDA(cudaLaunchKernel((const void*)kern, grid, dim3((unsigned)v.nt), args, tile_smem_bytes(v, rs.lut_shape()),
+                           stream));
+  return Status::Ok();
+}
+
 Status World::launch_tiles(int f0, int k, const TileVariant* v, bool commit) {
   if (!v || v->kmax < k) return {SE_ERR_INVALID_ARGUMENT, "no kernel variant for this many frames per launch"};
-  cudaKernel_t kern = rs->module->get(v->name());
-  const uint32_t* src = buf[cur];
-  uint32_t* dst = buf[cur ^ 1];
-  int Wv = W, Hv = H;
-  const uint16_t* lut = rs->d_lut;
-  void* args[] = {(void*)&src, (void*)&dst, &Wv, &Hv, &f0, &k, (void*)&lut};
-  dim3 grid((unsigned)((W + v->tw - 1) / v->tw), (unsigned)((H + v->th - 1) / v->th));
-  const size_t smem = tile_smem_bytes(*v, rs->lut_shape());
   Timed* t = nullptr;
   if (timing) {
     if (timed_used == timed.size()) {
@@ -163,7 +179,8 @@ Status World::launch_tiles(int f0, int k, const TileVariant* v, bool commit) {
     t->frames = k;
     SE_CUDA(cudaEventRecord(t->a, stream));
   }
-  SE_CUDA(cudaLaunchKernel((const void*)kern, grid, dim3((unsigned)v->nt), args, smem, stream));
+  Status s = launch_tile_kernel(*rs, *v, buf[cur], buf[cur ^ 1], W, wh, f0, k, ya, ya + H, stream);
+  if (!s.ok()) return s;
   if (t) SE_CUDA(cudaEventRecord(t->b, stream));
   if (commit) cur ^= 1;
   return Status::Ok();
@@ -189,11 +206,11 @@ Status World::timing_read(double* ms, long long* launches, long long* cell_frame
 }
 
 Status World::launch_edit(const se_modification* mods, int nlive) {
-  return launch_edit_on(*rs, buf[cur], W, H, mods, nlive, stream);
+  return launch_edit_on(*rs, buf[cur], W, ya, H, mods, nlive, stream);
 }
 
-Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int H, const se_modification* mods, int nlive,
-                      cudaStream_t stream) {
+Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int row0, int rows, const se_modification* mods,
+                      int nlive, cudaStream_t stream) {
   EditParams p;
   memset(&p, 0, sizeof p);
   long long total = 0;
@@ -211,12 +228,12 @@ Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int H, const se_
     int64_t rad = m.mod_size < 0 ? -(int64_t)m.mod_size : m.mod_size;
     bool normal = rad < (1 << 22) && m.position[0] > -(1 << 30) && m.position[0] < (1 << 30) &&
                   m.position[1] > -(1 << 30) && m.position[1] < (1 << 30);
-    int64_t x0 = 0, y0 = 0, x1 = W - 1, y1 = H - 1;
+    int64_t x0 = 0, y0 = row0, x1 = W - 1, y1 = (int64_t)row0 + rows - 1;
     if (normal) {
       x0 = std::max<int64_t>(0, m.position[0] - rad);
       x1 = std::min<int64_t>(W - 1, m.position[0] + rad);
-      y0 = std::max<int64_t>(0, m.position[1] - rad);
-      y1 = std::min<int64_t>(H - 1, m.position[1] + rad);
+      y0 = std::max<int64_t>(row0, m.position[1] - rad);
+      y1 = std::min<int64_t>((int64_t)row0 + rows - 1, m.position[1] + rad);
     }
     p.start[i] = total;
     if (x1 >= x0 && y1 >= y0) {
@@ -236,8 +253,8 @@ Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int H, const se_
   if (total == 0) return Status::Ok();
   cudaKernel_t kern = rs.module->get("se_edit");
   uint32_t* g = grid;
-  int Wv = W, Hv = H, n = nlive;
-  void* args[] = {(void*)&g, &Wv, &Hv, &n, &total, &p};
+  int Wv = W, Hv = row0 + rows, n = nlive, r0 = row0;
+  void* args[] = {(void*)&g, &Wv, &Hv, &n, &total, &p, &r0};
   dim3 blocks((unsigned)((total + 255) / 256));
   SE_CUDA(cudaLaunchKernel((const void*)kern, blocks, dim3(256), args, 0, stream));
   return Status::Ok();
@@ -247,6 +264,8 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
   if (nframes < 0) return {SE_ERR_INVALID_ARGUMENT, "nframes must be >= 0"};
   if (nmods < 0 || (nmods > 0 && !mods)) return {SE_ERR_INVALID_ARGUMENT, "bad modification list"};
   if ((int64_t)frame + nframes > INT32_MAX) return {SE_ERR_INVALID_ARGUMENT, "frame counter would overflow i32"};
+  if (halo >= 0 && nframes > halo)
+    return {SE_ERR_INVALID_ARGUMENT, "a band advances at most `halo` frames between halo exchanges"};
   int nlive = 0;
   const int nseen = std::min(nmods, SE_MAX_MODIFICATIONS);  // simulation.rs:205
   while (nlive < nseen && mods[nlive].mod_size != 0) ++nlive;  // falling_sand.glsl:139-141

@@ -54,7 +54,11 @@ static_assert(sizeof(EditParams) == 14352, "must match the device struct");
 
 struct World {
   std::shared_ptr<Ruleset> rs;
-  int W = 0, H = 0;
+  int W = 0, H = 0;  // buffer size: the whole world, or a band with its halo rows
+  // A band of a taller world (halo >= 0): the buffers hold world rows [ya, ya + H) of a
+  // W x wh world, the band's own rows plus up to `halo` rows either side.  Whole world:
+  // wh = H, ya = 0, halo = -1.
+  int wh = 0, ya = 0, halo = -1;
   int32_t frame = 0;
   uint32_t* buf[2] = {nullptr, nullptr};
   int cur = 0;
@@ -65,6 +69,8 @@ struct World {
   const TileVariant* single = nullptr;  // variant for one-frame launches (edit frames)
   ~World();
   Status create(std::shared_ptr<Ruleset> r, int w, int h);
+  // The band [row0, row0 + rows) of a w x world_h world with `halo` rows either side.
+  Status create_band(std::shared_ptr<Ruleset> r, int w, int world_h, int row0, int rows, int halo);
   Status step(int nframes, const se_modification* mods, int nmods);
   // k frames with counters f0.. from buf[cur] into buf[cur^1]; commit=false leaves cur
   // (the world's state) unchanged, for tuning trials.
@@ -88,9 +94,16 @@ struct World {
   Status histogram(unsigned long long* counts, int nbins);
 };
 
-// The edit pass (se_edit) for `nlive` mods over a W x H grid.
-Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int H, const se_modification* mods, int nlive,
-                      cudaStream_t stream);
+// One launch of a single-world tile kernel (se_tile_*): k frames with counters f0.. over
+// the world rows [ya, yb) of a W x H world held by src / dst (the whole world: 0, H).  The
+// one place that builds this kernel's argument list.
+Status launch_tile_kernel(const Ruleset& rs, const TileVariant& v, const uint32_t* src, uint32_t* dst, int W, int H,
+                          int f0, int k, int ya, int yb, cudaStream_t stream);
+
+// The edit pass (se_edit) for `nlive` mods over world rows [row0, row0 + rows) of a W-wide
+// world, held by `grid`.
+Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int row0, int rows, const se_modification* mods,
+                      int nlive, cudaStream_t stream);
 
 cudaError_t grid_digest(const uint32_t* g, unsigned long long n, unsigned long long* d_out, cudaStream_t s);
 cudaError_t grid_histogram(const uint32_t* g, unsigned long long n, int nbins, unsigned long long* d_counts,

@@ -36,9 +36,9 @@ std::string kernel_source(const std::string& generated_rules) {
   for (const TileVariant& t : tile_variants()) {
     o << "extern \"C\" __global__ void __launch_bounds__(" << t.nt << ") " << t.name()
       << "(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W, int H, int f0, int k,"
-         " const uint16_t* __restrict__ lut) {\n"
+         " const uint16_t* __restrict__ lut, int ya, int yb) {\n"
       << "  se_tile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
-      << ">(src, dst, W, H, f0, k, lut);\n}\n";
+      << ">(src, dst, W, H, f0, k, lut, ya, yb);\n}\n";
     o << "extern \"C\" __global__ void __launch_bounds__(" << t.nt << ") " << t.multi_name()
       << "(const SeWorldDesc* __restrict__ worlds, const SeTileJob* __restrict__ jobs, int pass,"
          " int frames_done, int k, const uint16_t* __restrict__ lut) {\n"

@@ -360,7 +360,7 @@ Status Server::run_batched() {
       r.remaining -= k;
       cell_updates += (double)ss.W * ss.H * k;
       if (!r.started && !r.mods.empty()) {
-        st = launch_edit_on(*rs, ss.buf(ss.cur), ss.W, ss.H, r.mods.data(), (int)r.mods.size(), stream);
+        st = launch_edit_on(*rs, ss.buf(ss.cur), ss.W, 0, ss.H, r.mods.data(), (int)r.mods.size(), stream);
         if (!st.ok()) return st;
       }
       r.started = true;
@@ -392,9 +392,6 @@ Status Server::run_plain() {
       v1 = &t;
       break;
     }
-  const size_t smem = tile_smem_bytes(*v1, rs->lut_shape());
-  cudaKernel_t kern = rs->module->get(v1->name());
-  const uint16_t* lut = rs->d_lut;
   cudaEvent_t t0;
   SE_CUDA(cudaEventCreate(&t0));
   SE_CUDA(cudaEventRecord(t0, stream));
@@ -415,15 +412,11 @@ Status Server::run_plain() {
       if (f == 1) {
         SE_CUDA(cudaMemsetAsync(ss.buf(ss.cur), 0, (size_t)ss.W * ss.H * 4, stream));
       } else {
-        const uint32_t* src = ss.buf(ss.cur);
-        uint32_t* dst = ss.buf(ss.cur ^ 1);
-        int W = ss.W, H = ss.H, f0 = f, k = 1;
-        void* args[] = {(void*)&src, (void*)&dst, &W, &H, &f0, &k, (void*)&lut};
-        dim3 grid((unsigned)((W + v1->tw - 1) / v1->tw), (unsigned)((H + v1->th - 1) / v1->th));
-        SE_CUDA(cudaLaunchKernel((const void*)kern, grid, dim3((unsigned)v1->nt), args, smem, stream));
+        st = launch_tile_kernel(*rs, *v1, ss.buf(ss.cur), ss.buf(ss.cur ^ 1), ss.W, ss.H, f, 1, 0, ss.H, stream);
+        if (!st.ok()) return st;
         ss.cur ^= 1;
         if (i == 0 && !r.mods.empty()) {
-          st = launch_edit_on(*rs, ss.buf(ss.cur), ss.W, ss.H, r.mods.data(), (int)r.mods.size(), stream);
+          st = launch_edit_on(*rs, ss.buf(ss.cur), ss.W, 0, ss.H, r.mods.data(), (int)r.mods.size(), stream);
           if (!st.ok()) return st;
         }
       }

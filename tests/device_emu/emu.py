@@ -49,12 +49,13 @@ extern "C" int emu_build_lut() {
 #endif
 }
 #define EMU_TILE(TW, TH, K) \
-extern "C" void emu_tile_##TW##x##TH##_k##K(const uint32_t* src, uint32_t* dst, int W, int H, int f0, int k) { \
+extern "C" void emu_tile_##TW##x##TH##_k##K(const uint32_t* src, uint32_t* dst, int W, int H, int f0, int k, \
+                                           int ya, int yb) { \
   blockDim.x = 1; threadIdx.x = 0; \
-  for (unsigned by = 0; by < (unsigned)((H + TH - 1) / TH); ++by) \
+  for (unsigned by = 0; by < (unsigned)((yb - ya + TH - 1) / TH); ++by) \
     for (unsigned bx = 0; bx < (unsigned)((W + TW - 1) / TW); ++bx) { \
       blockIdx.x = bx; blockIdx.y = by; \
-      se_tile_impl<TW, TH, K, 1>(src, dst, W, H, f0, k, g_lut); \
+      se_tile_impl<TW, TH, K, 1>(src, dst, W, H, f0, k, g_lut, ya, yb); \
     } \
 }
 @TILES@
@@ -95,7 +96,7 @@ extern "C" void emu_edit(uint32_t* grid, int W, int H, int nmods, long long tota
   for (long long t = 0; t < total; ++t) {
     blockIdx.x = (unsigned)(t / 256);
     threadIdx.x = (unsigned)(t % 256);
-    se_edit(grid, W, H, nmods, total, p);
+    se_edit(grid, W, H, nmods, total, p, 0);
   }
 }
 '''
@@ -131,15 +132,17 @@ class Emu:
         self.nmat = ruleset.num_materials
         self.has_lut = bool(self.lib.emu_build_lut())
 
-    def tiles(self, src: np.ndarray, f0: int, k: int, variant=None) -> np.ndarray:
-        """k frames (counters f0..f0+k-1) with one launch of the tile kernel."""
+    def tiles(self, src: np.ndarray, f0: int, k: int, variant=None, band=None) -> np.ndarray:
+        """k frames (counters f0..f0+k-1) with one launch of the tile kernel.  With
+        ``band = (world_height, ya)``, ``src`` holds world rows [ya, ya + src rows)."""
         if variant is None:
             variant = min((v for v in VARIANTS if v[2] >= k), key=lambda v: v[2])
         fn = getattr(self.lib, "emu_tile_%dx%d_k%d" % variant)
-        fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
-        H, W = src.shape
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 6
+        rows, W = src.shape
+        H, ya = band if band else (rows, 0)
         dst = np.zeros_like(src)
-        fn(src.ctypes.data, dst.ctypes.data, W, H, f0, k)
+        fn(src.ctypes.data, dst.ctypes.data, W, H, f0, k, ya, ya + rows)
         return dst
 
     def batch(self, grids, frames0, F, k, resident, variant=(128, 64, 8)):

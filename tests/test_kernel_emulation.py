@@ -117,3 +117,29 @@ def test_static_key_bitset(se, rulesets, name):
     assert np.array_equal(got, want)
     assert got[0]
     assert 0 < got.sum() < keys
+
+
+@pytest.mark.parametrize("name", ["four_materials", "twelve_materials"])
+def test_band_window_matches_port(emus, ports, name):
+    """A band buffer (world rows [ya, yb) of a taller world) advanced by the tile kernel in
+    window mode: after n frames, in one or several launches, every row at least n rows
+    inside the buffer equals the whole world run by the port (world coordinates for the
+    hash, the block parity and the border)."""
+    E, P = emus[name], ports[name]
+    W, H = 264, 230
+    g0 = _world(name, W, H, 21)
+    for ya, yb, launches, v in ((40, 130, (8,), (128, 64, 8)), (0, 90, (3, 5), (128, 64, 8)),
+                                (150, 230, (4, 4), (64, 64, 4)), (62, 200, (1, 1, 2), (128, 32, 1)),
+                                (62, 200, (16,), (128, 128, 16))):
+        f0 = 6
+        buf = g0[ya:yb].copy()
+        want = g0.copy()
+        n = 0
+        for k in launches:
+            vv = v if v[2] >= k else min((x for x in VARIANTS if x[2] >= k), key=lambda x: x[2])
+            buf = E.tiles(buf, f0 + n, k, vv, band=(H, ya))
+            n += k
+        P.run(want, f0 - 1, n)
+        lo = 0 if ya == 0 else n
+        hi = (yb - ya) if yb == H else (yb - ya) - n
+        assert np.array_equal(buf[lo:hi], want[ya + lo:ya + hi]), f"band [{ya}, {yb}) launches {launches}"
