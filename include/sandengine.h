@@ -108,6 +108,22 @@ void se_ruleset_free(se_ruleset* rs);
 int se_world_create(se_ruleset* rs, int width, int height, se_world** out);
 void se_world_destroy(se_world* w);
 
+/* ---- colour and light (the other two outputs of the reference's setCell,
+ * operations.glsl:99-169; Simulation::output_color / output_light, simulation.rs:110-114) ----
+ * se_world_set_light(w, 1) keeps a light field (RGBA32F per cell, zero at first, as the
+ * reference's textures are): every later se_world_step frame is followed by the light pass
+ * (a cell's light is its new material's emission if it emits, the sky value on row 0,
+ * else a blend of its 8 neighbours' previous light, masked by their old cells).  Light on
+ * makes every frame a separate launch.  0 frees the field. */
+int se_world_set_light(se_world* w, int enable);
+/* The current light field to / from a host or device buffer of width * height * 4 floats. */
+int se_world_get_light(se_world* w, float* rgba, size_t n_floats);
+int se_world_set_light_field(se_world* w, const float* rgba, size_t n_floats);
+/* output_color of the current grid (RGBA32F, width * height * 4 floats, host or device
+ * buffer): the material colour, darkened by noise(pos) / 4 for every material but EMPTY.
+ * The noise field is computed on the first call and kept. */
+int se_world_render_color(se_world* w, float* rgba, size_t n_floats);
+
 /* ---- row bands of one world (no counterpart in the reference, which runs one world on
  * one GPU) ------------------------------------------------------------------------------
  * A band world holds rows [row0, row0 + rows) of a width x world_height world plus up to

@@ -142,7 +142,26 @@ class Port:
         self.lib.port_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         self.lib.port_hash43.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        self.lib.port_color.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        self.lib.port_light.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int]
         self.num_materials = self.lib.port_num_materials()
+
+    def color(self, grid: np.ndarray) -> np.ndarray:
+        """output_color of a grid: (H, W, 4) float32 RGBA."""
+        g = np.ascontiguousarray(grid, dtype=np.uint32)
+        out = np.empty(g.shape + (4,), dtype=np.float32)
+        self.lib.port_color(g.ctypes.data, g.shape[1], g.shape[0], out.ctypes.data)
+        return out
+
+    def light(self, old: np.ndarray, new: np.ndarray, light_in: np.ndarray) -> np.ndarray:
+        """output_light of the frame that took ``old`` to ``new``, from the previous light
+        field ``light_in``: (H, W, 4) float32."""
+        o = np.ascontiguousarray(old, dtype=np.uint32)
+        n = np.ascontiguousarray(new, dtype=np.uint32)
+        li = np.ascontiguousarray(light_in, dtype=np.float32)
+        out = np.empty(o.shape + (4,), dtype=np.float32)
+        self.lib.port_light(o.ctypes.data, n.ctypes.data, li.ctypes.data, out.ctypes.data, o.shape[1], o.shape[0])
+        return out
 
     def step(self, grid: np.ndarray, frame: int, mods=None, nthreads: int = 1) -> None:
         """In place: one frame with counter value ``frame``."""

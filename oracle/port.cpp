@@ -9,6 +9,9 @@
 //   shaders/compute/operations.glsl:25-34      getMargolusOffset
 //   shaders/compute/operations.glsl:45-57      getCell with SCREEN_IS_BORDER (WALL outside)
 //   shaders/compute/math.glsl:28-38,74-79      hash4i / hash43
+// and the two other outputs of setCell (port_color, port_light):
+//   shaders/compute/operations.glsl:99-169     colour with noise, light propagation
+//   shaders/compute/math.glsl:40-44,82-106     old_hash2, _noise, noise
 // The per-ruleset part (TYPE_/MAT_ defines, isType_ checkers, rule_* functions and the
 // apply*Rules callers) is the GLSL text the oracle front end emits for the rule set,
 // rewritten by oracle/glsl2cpp.py and compiled through oracle/glsl_shim.hpp.
@@ -255,6 +258,138 @@ SE_EXPORT void port_run(uint32_t* grid, int W, int H, int frame0, int nframes, c
               int nmods, int nthreads) {
   for (int k = 0; k < nframes; ++k)
     port_step(grid, W, H, frame0 + k + 1, k == 0 ? mods : nullptr, k == 0 ? nmods : 0, nthreads);
+}
+
+// ---- colour and light (the rest of setCell, operations.glsl:99-169) ---------------------
+// Scalar restatement in the shader's evaluation order (dot products left to right,
+// max(a, b) = a < b ? b : a, mix(x, y, a) = x * (1 - a) + y * a), compiled without
+// contraction, so the compiled reference shader gives the same bits on the same libm.
+
+}  // extern "C"
+namespace {
+
+// math.glsl:40-44 old_hash2, one component: -1 + 2 * fract(sin(q) * 43758.5453123).
+inline float grad_component(float q) {
+  const float v = sin(q) * 43758.5453123f;
+  return -1.0f + 2.0f * fract(v);
+}
+
+// math.glsl:82-96 _noise (2D simplex noise with the sin-based gradient hash).
+inline float simplex(float px, float py) {
+  const float K1 = 0.366025404f, K2 = 0.211324865f;
+  const float s = (px + py) * K1;
+  const float ix = floor(px + s), iy = floor(py + s);
+  const float t = (ix + iy) * K2;
+  const float ax = (px - ix) + t, ay = (py - iy) + t;
+  const float m = step(ay, ax);
+  const float ox = m, oy = 1.0f - m;
+  const float bx = (ax - ox) + K2, by = (ay - oy) + K2;
+  const float c2 = 2.0f * K2;
+  const float cx = (ax - 1.0f) + c2, cy = (ay - 1.0f) + c2;
+  const float h0 = max(0.5f - (ax * ax + ay * ay), 0.0f);
+  const float h1 = max(0.5f - (bx * bx + by * by), 0.0f);
+  const float h2 = max(0.5f - (cx * cx + cy * cy), 0.0f);
+  // gradients at the three corners i, i + o, i + 1 (old_hash2: dot with (127.1, 311.7) and
+  // (269.5, 183.3))
+  auto grad = [](float qx, float qy, float& gx, float& gy) {
+    gx = grad_component(qx * 127.1f + qy * 311.7f);
+    gy = grad_component(qx * 269.5f + qy * 183.3f);
+  };
+  float g0x, g0y, g1x, g1y, g2x, g2y;
+  grad(ix, iy, g0x, g0y);
+  grad(ix + ox, iy + oy, g1x, g1y);
+  grad(ix + 1.0f, iy + 1.0f, g2x, g2y);
+  const float n0 = h0 * h0 * h0 * h0 * (ax * g0x + ay * g0y);
+  const float n1 = h1 * h1 * h1 * h1 * (bx * g1x + by * g1y);
+  const float n2 = h2 * h2 * h2 * h2 * (cx * g2x + cy * g2y);
+  return 0.25f + 0.5f * (n0 * 70.0f + n1 * 70.0f + n2 * 70.0f);
+}
+
+// math.glsl:98-106 noise(p, octaves = 3, lacunarity = 2, frequency = 0.25), as setCell calls it.
+inline float cell_noise(float px, float py) {
+  float f = 0.0f;
+  for (int o = 1; o < 4; ++o) {
+    f = f + (1.0f / (float)o) * simplex(px * 0.25f, py * 0.25f);
+    px = px * 2.0f;
+    py = py * 2.0f;
+  }
+  return f;
+}
+
+// operations.glsl:68-70
+inline bool light_obstacle(const Material& m, ivec2 p) {
+  return m.emission.x == 0.0f && m.emission.y == 0.0f && m.emission.z == 0.0f && !isType_EMPTY(Cell(m, p));
+}
+
+}  // namespace
+extern "C" {
+
+// output_color for a grid (operations.glsl:100-108): the material colour, darkened by
+// noise(pos) / 4 and clamped to [0, 1] for every material but EMPTY.  RGBA per cell.
+SE_EXPORT void port_color(const uint32_t* grid, int W, int H, float* out) {
+  init_table();
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const Material mt = material_from_id(grid[(int64_t)y * W + x]);
+      vec4 c = mt.color;
+      if (!(mt == MAT_EMPTY)) {
+        const float r = cell_noise((float)x, (float)y) * 0.25f;
+        c.x = clamp(c.x - r, 0.0f, 1.0f);
+        c.y = clamp(c.y - r, 0.0f, 1.0f);
+        c.z = clamp(c.z - r, 0.0f, 1.0f);
+      }
+      float* o = out + 4 * ((int64_t)y * W + x);
+      o[0] = c.x;
+      o[1] = c.y;
+      o[2] = c.z;
+      o[3] = c.w;
+    }
+}
+
+// output_light of one frame (operations.glsl:114-166): the new cell's emission if it
+// emits; the sky value on row 0; else the mean of the 8 neighbours' light (the previous
+// frame's, with its colour masked where the neighbour's old cell is a light obstacle),
+// blended half-way towards their per-channel maximum.  old/new: the grids before and
+// after the frame; RGBA per cell.
+SE_EXPORT void port_light(const uint32_t* old_grid, const uint32_t* new_grid, const float* lin, float* lout, int W,
+                          int H) {
+  init_table();
+  static const int dx[8] = {0, 0, -1, -1, 1, 1, 1, -1};  // math.glsl:154-166 order
+  static const int dy[8] = {1, -1, 1, -1, 1, -1, 0, 0};
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const Material nm = material_from_id(new_grid[(int64_t)y * W + x]);
+      float L[4];
+      if (nm.emission.x != 0.0f || nm.emission.y != 0.0f || nm.emission.z != 0.0f) {
+        L[0] = nm.emission.x, L[1] = nm.emission.y, L[2] = nm.emission.z, L[3] = nm.emission.w;
+      } else if (y == 0) {
+        L[0] = L[1] = L[2] = 1.0f;
+        L[3] = 0.999999f;
+      } else {
+        float avg[4] = {0, 0, 0, 0}, mx[4] = {0, 0, 0, 0}, maxf = 0.0f;
+        int num = 0;
+        for (int n = 0; n < 8; ++n) {
+          const int qx = x + dx[n], qy = y + dy[n];
+          if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+          const int64_t q = (int64_t)qy * W + qx;
+          const float keep = light_obstacle(material_from_id(old_grid[q]), ivec2(qx, qy)) ? 0.0f : 1.0f;
+          const float* l = lin + 4 * q;
+          const float r = l[0] * keep, g = l[1] * keep, b = l[2] * keep, a = l[3] * 1.0f;
+          const float falloff = a == 0.0f ? maxf : a;
+          const float t[4] = {r * a, g * a, b * a, falloff};
+          for (int c = 0; c < 4; ++c) avg[c] = avg[c] + t[c];
+          maxf = max(falloff, maxf);
+          ++num;
+          for (int c = 0; c < 4; ++c) mx[c] = max(mx[c], t[c]);
+        }
+        if (num > 0)
+          for (int c = 0; c < 4; ++c) avg[c] = avg[c] / (float)num;
+        for (int c = 0; c < 3; ++c) L[c] = avg[c] * (1.0f - 0.5f) + mx[c] * 0.5f;
+        L[3] = avg[3];
+      }
+      float* o = lout + 4 * ((int64_t)y * W + x);
+      for (int c = 0; c < 4; ++c) o[c] = L[c];
+    }
 }
 
 // hash43 lanes, exposed for known-answer tests of the RNG.

@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["lang/yaml.cpp", "lang/lang.cpp", "lang/codegen.cpp", "runtime/jit.cpp",
                 "runtime/engine.cpp", "runtime/batch.cpp", "runtime/server.cpp", "runtime/snapshot.cpp",
                 "capi.cpp"]
-CUDA_SOURCES = ["kernels/devutil.cu"]
+CUDA_SOURCES = ["kernels/devutil.cu", "kernels/render.cu"]
 EMBED = [("SE_PRELUDE_SRC", "kernels/prelude.cuh"), ("SE_MARGOLUS_SRC", "kernels/margolus.cuh")]
 
 

@@ -218,6 +218,51 @@ SE_API int se_world_copy_rows(se_world* w, int row, int nrows, void* ptr, int to
   });
 }
 
+SE_API int se_world_set_light(se_world* w, int enable) {
+  return guard([&] {
+    if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
+    return ret(w->w->set_light(enable != 0));
+  });
+}
+
+// Copies between the current light field (device) and a host or device RGBA32F buffer.
+static int light_copy(se_world* w, void* p, size_t n_floats, bool to_world) {
+  if (!w || !p) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+  auto& W = *w->w;
+  if (!W.light[0]) return fail(SE_ERR_INVALID_ARGUMENT, "the light field is off (se_world_set_light)");
+  const size_t need = (size_t)W.W * W.H * 4;
+  if (n_floats < need) return fail(SE_ERR_INVALID_ARGUMENT, "buffer smaller than width * height * 4 floats");
+  float4* l = W.light[W.lcur];
+  cudaError_t e = to_world ? cudaMemcpyAsync(l, p, need * 4, cudaMemcpyDefault, W.stream)
+                           : cudaMemcpyAsync(p, l, need * 4, cudaMemcpyDefault, W.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(W.stream);
+  if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+  return (int)SE_OK;
+}
+
+SE_API int se_world_get_light(se_world* w, float* rgba, size_t n_floats) {
+  return guard([&] { return light_copy(w, rgba, n_floats, false); });
+}
+
+SE_API int se_world_set_light_field(se_world* w, const float* rgba, size_t n_floats) {
+  return guard([&] { return light_copy(w, const_cast<float*>(rgba), n_floats, true); });
+}
+
+SE_API int se_world_render_color(se_world* w, float* rgba, size_t n_floats) {
+  return guard([&] {
+    if (!w || !rgba) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    auto& W = *w->w;
+    const size_t need = (size_t)W.W * W.H * 4;
+    if (n_floats < need) return fail(SE_ERR_INVALID_ARGUMENT, "buffer smaller than width * height * 4 floats");
+    se::rt::Status s = W.render_color();
+    if (!s.ok()) return ret(s);
+    cudaError_t e = cudaMemcpyAsync(rgba, W.d_color, need * 4, cudaMemcpyDefault, W.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(W.stream);
+    if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    return (int)SE_OK;
+  });
+}
+
 SE_API int se_world_create(se_ruleset* rs, int width, int height, se_world** out) {
   return guard([&] {
     if (!rs || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");

@@ -1,0 +1,173 @@
+// Colour and light passes (the reference's setCell outputs other than the cell id),
+// shaders/compute/operations.glsl:99-169 with math.glsl:40-44,82-106.
+//
+// Every float operation is an explicit round-to-nearest intrinsic in the shader's order, so
+// nothing is contracted into FMAs: the light pass equals a strict-IEEE CPU evaluation bit
+// for bit.  The colour's noise calls sinf (CUDA's, not a fast approximation); the
+// reference's GLSL sin is driver-defined, so colours agree with a CPU evaluation only
+// within the error that a last-place difference of sin leaves after the gradient hash.
+#include "render.hpp"
+
+#include <algorithm>
+
+namespace se::rt {
+namespace {
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+// GLSL max / min / clamp as the spec defines them (max(a, b) = a < b ? b : a)
+__device__ __forceinline__ float gmax(float a, float b) { return a < b ? b : a; }
+__device__ __forceinline__ float gmin(float a, float b) { return b < a ? b : a; }
+__device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+
+// old_hash2 component: -1 + 2 * fract(sin(q) * 43758.5453123)
+__device__ __forceinline__ float grad_component(float q) {
+  const float v = fmul(sinf(q), 43758.5453123f);
+  return fadd(-1.0f, fmul(2.0f, fsub(v, floorf(v))));
+}
+__device__ __forceinline__ void grad(float qx, float qy, float& gx, float& gy) {
+  gx = grad_component(fadd(fmul(qx, 127.1f), fmul(qy, 311.7f)));
+  gy = grad_component(fadd(fmul(qx, 269.5f), fmul(qy, 183.3f)));
+}
+
+// _noise: 2D simplex noise
+__device__ float simplex(float px, float py) {
+  const float K1 = 0.366025404f, K2 = 0.211324865f;
+  const float s = fmul(fadd(px, py), K1);
+  const float ix = floorf(fadd(px, s)), iy = floorf(fadd(py, s));
+  const float t = fmul(fadd(ix, iy), K2);
+  const float ax = fadd(fsub(px, ix), t), ay = fadd(fsub(py, iy), t);
+  const float m = ax < ay ? 0.0f : 1.0f;  // step(a.y, a.x)
+  const float ox = m, oy = fsub(1.0f, m);
+  const float bx = fadd(fsub(ax, ox), K2), by = fadd(fsub(ay, oy), K2);
+  const float c2 = fmul(2.0f, K2);
+  const float cx = fadd(fsub(ax, 1.0f), c2), cy = fadd(fsub(ay, 1.0f), c2);
+  const float h0 = gmax(fsub(0.5f, fadd(fmul(ax, ax), fmul(ay, ay))), 0.0f);
+  const float h1 = gmax(fsub(0.5f, fadd(fmul(bx, bx), fmul(by, by))), 0.0f);
+  const float h2 = gmax(fsub(0.5f, fadd(fmul(cx, cx), fmul(cy, cy))), 0.0f);
+  float g0x, g0y, g1x, g1y, g2x, g2y;
+  grad(ix, iy, g0x, g0y);
+  grad(fadd(ix, ox), fadd(iy, oy), g1x, g1y);
+  grad(fadd(ix, 1.0f), fadd(iy, 1.0f), g2x, g2y);
+  const float n0 = fmul(fmul(fmul(fmul(h0, h0), h0), h0), fadd(fmul(ax, g0x), fmul(ay, g0y)));
+  const float n1 = fmul(fmul(fmul(fmul(h1, h1), h1), h1), fadd(fmul(bx, g1x), fmul(by, g1y)));
+  const float n2 = fmul(fmul(fmul(fmul(h2, h2), h2), h2), fadd(fmul(cx, g2x), fmul(cy, g2y)));
+  return fadd(0.25f, fmul(0.5f, fadd(fadd(fmul(n0, 70.0f), fmul(n1, 70.0f)), fmul(n2, 70.0f))));
+}
+
+__global__ void __launch_bounds__(256) se_noise_kernel(float* __restrict__ out, int W, int H) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (x >= W || y >= H) return;
+  float px = (float)x, py = (float)y, f = 0.0f;
+  for (int o = 1; o < 4; ++o) {  // noise(p, 3 octaves, lacunarity 2, frequency 0.25)
+    f = fadd(f, fmul(__fdiv_rn(1.0f, (float)o), simplex(fmul(px, 0.25f), fmul(py, 0.25f))));
+    px = fmul(px, 2.0f);
+    py = fmul(py, 2.0f);
+  }
+  out[(size_t)y * W + x] = f;
+}
+
+__device__ __forceinline__ uint32_t mat_index(uint32_t id, int nmat) { return id < (uint32_t)nmat ? id : 1u; }
+
+// One cell per thread, grid-stride: id, cached noise -> RGBA32F.
+__global__ void __launch_bounds__(256) se_color_kernel(const uint32_t* __restrict__ grid,
+                                                       const float* __restrict__ noise, float4* __restrict__ out,
+                                                       long long n, const RenderMat* __restrict__ mats, int nmat) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t m = mat_index(__ldg(grid + i), nmat);
+    const RenderMat* r = mats + m;
+    float4 c = make_float4(__ldg(r->color + 0), __ldg(r->color + 1), __ldg(r->color + 2), __ldg(r->color + 3));
+    if (__ldg(&r->flags) & kRenderNoise) {
+      const float d = fmul(__ldg(noise + i), 0.25f);
+      c.x = gclamp(fsub(c.x, d), 0.0f, 1.0f);
+      c.y = gclamp(fsub(c.y, d), 0.0f, 1.0f);
+      c.z = gclamp(fsub(c.z, d), 0.0f, 1.0f);
+    }
+    out[i] = c;
+  }
+}
+
+__global__ void __launch_bounds__(256) se_light_kernel(const uint32_t* __restrict__ old_grid,
+                                                       const uint32_t* __restrict__ new_grid,
+                                                       const float4* __restrict__ lin, float4* __restrict__ lout,
+                                                       int W, int H, const RenderMat* __restrict__ mats, int nmat) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (x >= W || y >= H) return;
+  const size_t i = (size_t)y * W + x;
+  const RenderMat* nm = mats + mat_index(__ldg(new_grid + i), nmat);
+  float4 L;
+  if (__ldg(&nm->flags) & kRenderEmits) {
+    L = make_float4(__ldg(nm->emission + 0), __ldg(nm->emission + 1), __ldg(nm->emission + 2),
+                    __ldg(nm->emission + 3));
+  } else if (y == 0) {
+    L = make_float4(1.0f, 1.0f, 1.0f, 0.999999f);
+  } else {
+    // neighbours in getDiagonalNeighbours order: DOWN, UP, DOWNLEFT, UPLEFT, DOWNRIGHT,
+    // UPRIGHT, RIGHT, LEFT
+    const int dx[8] = {0, 0, -1, -1, 1, 1, 1, -1}, dy[8] = {1, -1, 1, -1, 1, -1, 0, 0};
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f, m0 = 0.0f, m1 = 0.0f, m2 = 0.0f, maxf = 0.0f;
+    int num = 0;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const int qx = x + dx[n], qy = y + dy[n];
+      if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+      const size_t q = (size_t)qy * W + qx;
+      const uint32_t om = mat_index(__ldg(old_grid + q), nmat);
+      const float keep = (__ldg(&mats[om].flags) & kRenderObstacle) ? 0.0f : 1.0f;
+      const float4 l = __ldg(lin + q);
+      const float r = fmul(l.x, keep), g = fmul(l.y, keep), b = fmul(l.z, keep), a = fmul(l.w, 1.0f);
+      const float falloff = a == 0.0f ? maxf : a;
+      const float t0 = fmul(r, a), t1 = fmul(g, a), t2 = fmul(b, a), t3 = falloff;
+      a0 = fadd(a0, t0);
+      a1 = fadd(a1, t1);
+      a2 = fadd(a2, t2);
+      a3 = fadd(a3, t3);
+      maxf = gmax(falloff, maxf);
+      ++num;
+      m0 = gmax(m0, t0);
+      m1 = gmax(m1, t1);
+      m2 = gmax(m2, t2);  // the alpha of the maximum is not used (mix takes .rgb)
+    }
+    if (num > 0) {
+      const float fn = (float)num;
+      a0 = __fdiv_rn(a0, fn);
+      a1 = __fdiv_rn(a1, fn);
+      a2 = __fdiv_rn(a2, fn);
+      a3 = __fdiv_rn(a3, fn);
+    }
+    // mix(avg.rgb, max.rgb, 0.5) = avg * (1 - 0.5) + max * 0.5
+    L = make_float4(fadd(fmul(a0, 0.5f), fmul(m0, 0.5f)), fadd(fmul(a1, 0.5f), fmul(m1, 0.5f)),
+                    fadd(fmul(a2, 0.5f), fmul(m2, 0.5f)), a3);
+  }
+  lout[i] = L;
+}
+
+}  // namespace
+
+cudaError_t render_noise(float* noise, int W, int H, cudaStream_t s) {
+  dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
+  se_noise_kernel<<<grid, 256, 0, s>>>(noise, W, H);
+  return cudaGetLastError();
+}
+
+cudaError_t render_color(const uint32_t* grid, const float* noise, float4* out, int W, int H, const RenderMat* mats,
+                         int nmat, cudaStream_t s) {
+  const long long n = (long long)W * H;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long blocks = std::min<long long>((n + 255) / 256, (long long)sms * 8);
+  se_color_kernel<<<(unsigned)(blocks > 0 ? blocks : 1), 256, 0, s>>>(grid, noise, out, n, mats, nmat);
+  return cudaGetLastError();
+}
+
+cudaError_t light_pass(const uint32_t* old_grid, const uint32_t* new_grid, const float4* light_in, float4* light_out,
+                       int W, int H, const RenderMat* mats, int nmat, cudaStream_t s) {
+  dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
+  se_light_kernel<<<grid, 256, 0, s>>>(old_grid, new_grid, light_in, light_out, W, H, mats, nmat);
+  return cudaGetLastError();
+}
+
+}  // namespace se::rt

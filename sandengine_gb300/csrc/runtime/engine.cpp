@@ -2,6 +2,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <set>
 
 #include "../../../include/sandengine.h"
 
@@ -47,12 +48,32 @@ Status Ruleset::ensure_loaded() {
     SE_CUDA(cudaLaunchKernel((const void*)m->get("se_build_static"), dim3(sblocks), dim3(256), args, 0, nullptr));
     SE_CUDA(cudaDeviceSynchronize());
   }
+  {  // render table (operations.glsl:68-70, 100-108, 126): colour, emission and flags
+    std::set<std::string> empty_types = {"EMPTY"};  // isType_EMPTY: EMPTY and its child types
+    for (const auto& t : parsed.types)
+      if (t.name == "EMPTY") empty_types.insert(t.children.begin(), t.children.end());
+    std::vector<RenderMat> table(parsed.materials.size());
+    for (size_t i = 0; i < table.size(); ++i) {
+      const auto& mt = parsed.materials[i];
+      RenderMat& r = table[i];
+      memset(&r, 0, sizeof r);
+      for (int c = 0; c < 4; ++c) r.color[c] = mt.color[c], r.emission[c] = mt.emission[c];
+      const bool dark = mt.emission[0] == 0.0f && mt.emission[1] == 0.0f && mt.emission[2] == 0.0f;
+      if (!dark) r.flags |= kRenderEmits;  // vec3 != vec3(0.0): some component differs
+      if (dark && !empty_types.count(mt.mattype)) r.flags |= kRenderObstacle;
+      if (i != 0) r.flags |= kRenderNoise;  // mat != MAT_EMPTY
+    }
+    cudaError_t e = cudaMalloc(&d_render, table.size() * sizeof(RenderMat));
+    if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    SE_CUDA(cudaMemcpy(d_render, table.data(), table.size() * sizeof(RenderMat), cudaMemcpyHostToDevice));
+  }
   module = std::move(m);
   return Status::Ok();
 }
 
 Ruleset::~Ruleset() {
   if (d_lut) cudaFree(d_lut);
+  if (d_render) cudaFree(d_render);
 }
 
 World::~World() {
@@ -62,6 +83,10 @@ World::~World() {
   }
   if (buf[0]) cudaFree(buf[0]);
   if (buf[1]) cudaFree(buf[1]);
+  for (auto* l : light)
+    if (l) cudaFree(l);
+  if (d_noise) cudaFree(d_noise);
+  if (d_color) cudaFree(d_color);
   if (d_scratch) cudaFree(d_scratch);
   if (own_stream) cudaStreamDestroy(own_stream);
 }
@@ -281,6 +306,26 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
   }
   const TileVariant* vone = single ? single : pick_variant(1);
   const int kdef = steps_per_launch > 0 ? steps_per_launch : vmulti->kmax;
+  if (light[0]) {  // one frame at a time, each followed by the light pass
+    for (int i = 0; i < nframes; ++i) {
+      const int f = frame + 1 + i;
+      if (f == 1) {  // the clear goes to the spare buffer: the light pass reads the old grid
+        SE_CUDA(cudaMemsetAsync(buf[cur ^ 1], 0, (size_t)W * H * sizeof(uint32_t), stream));
+        cur ^= 1;
+      } else {
+        Status s = launch_tiles(f, 1, vone);
+        if (!s.ok()) return s;
+        if (i == 0 && nlive > 0) {
+          s = launch_edit(mods, nlive);
+          if (!s.ok()) return s;
+        }
+      }
+      Status s = light_frame();
+      if (!s.ok()) return s;
+    }
+    frame += nframes;
+    return Status::Ok();
+  }
   int i = 0;
   while (i < nframes) {
     const int f = frame + 1 + i;
@@ -303,6 +348,49 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
     i += k;
   }
   frame += nframes;
+  return Status::Ok();
+}
+
+Status World::set_light(bool on) {
+  if (on && halo >= 0) return {SE_ERR_INVALID_ARGUMENT, "the light field is not kept for bands"};
+  if (!on) {
+    for (auto*& l : light)
+      if (l) cudaFree(l), l = nullptr;
+    return Status::Ok();
+  }
+  if (light[0]) return Status::Ok();
+  const size_t bytes = (size_t)W * H * sizeof(float4);
+  for (auto*& l : light) {
+    cudaError_t e = cudaMalloc(&l, bytes);
+    if (e != cudaSuccess) {
+      set_light(false);
+      return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    }
+  }
+  SE_CUDA(cudaMemsetAsync(light[0], 0, bytes, stream));
+  lcur = 0;
+  return Status::Ok();
+}
+
+Status World::light_frame() {
+  SE_CUDA(light_pass(buf[cur ^ 1], buf[cur], light[lcur], light[lcur ^ 1], W, H, rs->d_render,
+                     rs->num_materials(), stream));
+  lcur ^= 1;
+  return Status::Ok();
+}
+
+Status World::render_color() {
+  if (halo >= 0) return {SE_ERR_INVALID_ARGUMENT, "colours are rendered for whole worlds"};
+  if (!d_noise) {
+    cudaError_t e = cudaMalloc(&d_noise, (size_t)W * H * sizeof(float));
+    if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    SE_CUDA(render_noise(d_noise, W, H, stream));
+  }
+  if (!d_color) {
+    cudaError_t e = cudaMalloc(&d_color, (size_t)W * H * sizeof(float4));
+    if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+  }
+  SE_CUDA(se::rt::render_color(buf[cur], d_noise, d_color, W, H, rs->d_render, rs->num_materials(), stream));
   return Status::Ok();
 }
 

@@ -10,6 +10,7 @@
 
 #include "../lang/codegen.hpp"
 #include "../lang/lang.hpp"
+#include "../kernels/render.hpp"
 #include "jit.hpp"
 
 struct se_modification;
@@ -36,6 +37,8 @@ struct Ruleset {
   // Block transition table (when cuda.lut_entries > 0), followed 16-byte aligned by the
   // bitset of static keys.
   uint16_t* d_lut = nullptr;
+  // Per-material colour / emission / flags for the colour and light passes.
+  RenderMat* d_render = nullptr;
   ~Ruleset();
   LutShape lut_shape() const { return {cuda.lut_entries, cuda.lut_static_words}; }
   int num_materials() const { return (int)parsed.materials.size(); }
@@ -92,6 +95,19 @@ struct World {
   Status timing_read(double* ms, long long* launches, long long* cell_frames, long long* cells);
   Status digest(unsigned long long* out);
   Status histogram(unsigned long long* counts, int nbins);
+
+  // Colour and light outputs of the reference's setCell (opt-in).  With light on, every
+  // frame runs as a one-frame launch followed by the light pass over the frame's old and
+  // new grids; light[lcur] is the current field (RGBA32F per cell, zero at creation as the
+  // reference's textures are).  The noise term of the colour depends only on the position
+  // and is computed once per world.
+  float4* light[2] = {nullptr, nullptr};
+  int lcur = 0;
+  float* d_noise = nullptr;
+  float4* d_color = nullptr;
+  Status set_light(bool on);
+  Status light_frame();  // light pass for the frame just taken (old grid buf[cur ^ 1])
+  Status render_color();  // the current grid's colours into d_color
 };
 
 // One launch of a single-world tile kernel (se_tile_*): k frames with counters f0.. over

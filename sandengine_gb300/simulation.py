@@ -155,6 +155,35 @@ class Simulation:
                                          ctypes.byref(c)))
         return {"kernel_ms": ms.value, "launches": n.value, "cell_frames": cf.value, "cells": c.value}
 
+    def set_light(self, enable: bool = True) -> None:
+        """Keep the light field (Simulation::output_light): each later frame is followed by
+        the light pass.  Starts at zero, as the reference's texture does."""
+        check(lib().se_world_set_light(self._h, 1 if enable else 0))
+
+    @property
+    def output_light(self) -> np.ndarray:
+        """The current light field, (H, W, 4) float32 RGBA."""
+        w, h = self.size
+        out = np.empty((h, w, 4), dtype=np.float32)
+        check(lib().se_world_get_light(self._h, out.ctypes.data, out.size))
+        return out
+
+    @output_light.setter
+    def output_light(self, rgba: np.ndarray) -> None:
+        w, h = self.size
+        a = np.ascontiguousarray(rgba, dtype=np.float32)
+        if a.shape != (h, w, 4):
+            raise ValueError(f"light must have shape {(h, w, 4)}")
+        check(lib().se_world_set_light_field(self._h, a.ctypes.data, a.size))
+
+    @property
+    def output_color(self) -> np.ndarray:
+        """Simulation::output_color of the current grid, (H, W, 4) float32 RGBA."""
+        w, h = self.size
+        out = np.empty((h, w, 4), dtype=np.float32)
+        check(lib().se_world_render_color(self._h, out.ctypes.data, out.size))
+        return out
+
     def digest(self) -> int:
         d = ctypes.c_uint64(0)
         check(lib().se_world_digest(self._h, ctypes.byref(d)))

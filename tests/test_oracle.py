@@ -138,3 +138,36 @@ def test_port_edit_pass_extreme_mods(rulesets):
         P.step(gp, f, mods)
         gr = R.step(gr, f, mods)
         assert np.array_equal(gp, gr)
+
+
+@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout")
+@pytest.mark.parametrize("name", ["reference", "twelve_materials"])
+def test_port_color_and_light_match_reference_shader(rulesets, name):
+    """The port's colour (material colour minus 3-octave noise) and light propagation equal
+    the compiled reference shader's output_color and output_light bit for bit, frame after
+    frame (the light field carried over), with edits, emitting materials (the twelve set
+    has two), the frame-1 clear and worlds wider than the noise period."""
+    text = rulesets[name]
+    P, R = Port(text), Ref(text)
+    rng = np.random.default_rng(11)
+    for H, W, f0 in ((40, 300, 2), (17, 23, 0)):
+        g = rng.integers(0, P.num_materials + 2, size=(H, W)).astype(np.uint32)
+        g[rng.random((H, W)) < 0.4] = 0
+        light = np.zeros((H, W, 4), dtype=np.float32)
+        port_light = light.copy()
+        gp = g.copy()
+        for f in range(f0 + 1, f0 + 25):
+            mods = None
+            if f % 4 == 0:
+                mods = [(int(rng.integers(0, W)), int(rng.integers(0, H)), int(rng.integers(0, 2)),
+                         int(rng.integers(1, 6)), int(rng.integers(0, P.num_materials))) for _ in range(4)]
+            color = np.zeros((H, W, 4), dtype=np.float32)
+            new = R.step(g, f, mods, light=light, color=color)
+            old = gp.copy()
+            P.step(gp, f, mods)
+            assert np.array_equal(gp, new)
+            port_light = P.light(old, gp, port_light)
+            assert np.array_equal(P.color(gp).view(np.uint32), color.view(np.uint32)), f"colour, frame {f}"
+            assert np.array_equal(port_light.view(np.uint32), light.view(np.uint32)), f"light, frame {f}"
+            g = new
+        assert np.count_nonzero(light) > 0
