@@ -52,6 +52,9 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--light", action="store_true",
+                    help="world workloads: keep the light field (light pass after every frame, one-frame "
+                         "launches) and render the colours once per step")
     return ap.parse_args()
 
 
@@ -234,9 +237,16 @@ def run_ours(args, rep):
         k = sim.autotune(3)
     stream = torch.cuda.ExternalStream(sim.stream)
     mods = [step_mods(se, wl, W, r, spec["edit_mats"]) for r in range(args.warmup + args.steps)]
+    if args.light:
+        sim.set_light(True)
+
+    def one_step(r):
+        sim.run_frames(FRAMES_PER_STEP, mods[r])
+        if args.light:
+            sim.render_color_device()
 
     for r in range(args.warmup):
-        sim.run_frames(FRAMES_PER_STEP, mods[r])
+        one_step(r)
     sim.synchronize()
 
     sim.set_timing(True)
@@ -247,12 +257,13 @@ def run_ours(args, rep):
     with ClockSampler(torch.cuda.current_device()) as clocks:
         start.record(stream)
         for r in range(args.steps):
-            sim.run_frames(FRAMES_PER_STEP, mods[args.warmup + r])
+            one_step(args.warmup + r)
         end.record(stream)
         torch.cuda.synchronize()
     rep.barrier()
     ms = start.elapsed_time(end)
     timing = sim.read_timing()
+    passes = {p: sim.read_pass_timing(p) for p in (1, 2)} if args.light else {}
     sim.set_timing(False)
     ms_max = rep.max(ms)
     updates = float(W) * H * FRAMES_PER_STEP * args.steps
@@ -268,7 +279,7 @@ def run_ours(args, rep):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for r in range(args.steps):
-            sim.run_frames(FRAMES_PER_STEP, mods[args.warmup + r])
+            one_step(args.warmup + r)
             check(lib().se_world_get_grid_async(sim.handle, host.data_ptr(), W * H))
         sim.synchronize()
         e2e_s = rep.max(time.perf_counter() - t0)
@@ -295,9 +306,19 @@ def run_ours(args, rep):
                      "kernel": f"se_tile (k={k})", "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": alg_bytes_per_launch,
                      "avg_launch_ms": avg_launch_s * 1e3, "kernel_share_of_step": kernel_ms / ms if ms else None},
-        "gpu_launches": launches + args.steps,
+        "gpu_launches": launches + args.steps + sum(p["launches"] for p in passes.values()),
         "clocks": clocks.summary(),
     }
+    for p, name, bpc in ((1, "light_pass", 40.0), (2, "color_pass", 24.0)):
+        if p in passes and passes[p]["launches"]:
+            t = passes[p]
+            avg_s = t["kernel_ms"] / t["launches"] / 1e3
+            ach = bpc * t["cells"] / t["launches"] / avg_s / 1e9
+            out[name] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "algorithmic_bytes_per_cell": bpc, "launches": t["launches"], "avg_launch_ms": avg_s * 1e3,
+                         "share_of_step": t["kernel_ms"] / ms if ms else None}
+    if args.light:
+        out["config"]["workload"] += "; light field kept (light pass after every frame) and colours rendered once per step"
     if e2e:
         out["e2e"] = e2e
     if rep.rank == 0 and rep.world_size == 1 and not args.no_cpu_baseline:

@@ -123,6 +123,9 @@ int se_world_set_light_field(se_world* w, const float* rgba, size_t n_floats);
  * buffer): the material colour, darkened by noise(pos) / 4 for every material but EMPTY.
  * The noise field is computed on the first call and kept. */
 int se_world_render_color(se_world* w, float* rgba, size_t n_floats);
+/* The same into the world's own device buffer, ordered on the world's stream (no
+ * synchronization); *rgba stays valid until the next render or se_world_destroy. */
+int se_world_render_color_device(se_world* w, float** rgba);
 
 /* ---- row bands of one world (no counterpart in the reference, which runs one world on
  * one GPU) ------------------------------------------------------------------------------
@@ -208,6 +211,9 @@ int se_grid_histogram_noalloc(const uint32_t* device_cells, uint64_t count, int 
 int se_world_set_timing(se_world* w, int enable);
 int se_world_read_timing(se_world* w, double* kernel_ms, long long* launches, long long* cell_frames,
                          long long* cells);
+/* The same for the light pass (pass = 1; algorithmic bytes 40 x cells: old and new id, old
+ * and new RGBA32F light) and the colour pass (pass = 2; 24 x cells: id, noise, RGBA32F). */
+int se_world_read_pass_timing(se_world* w, int pass, double* kernel_ms, long long* launches, long long* cells);
 
 /* ---- many worlds (no counterpart in the reference, which runs one world) --------------- */
 

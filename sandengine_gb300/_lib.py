@@ -58,9 +58,12 @@ _SIGS = {
     "se_ruleset_num_materials": ([_P, ctypes.POINTER(_I)], _I),
     "se_ruleset_material_id": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
     "se_world_set_light": ([_P, _I], _I),
+    "se_world_read_pass_timing": ([_P, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
+                                   ctypes.POINTER(ctypes.c_longlong)], _I),
     "se_world_get_light": ([_P, _P, ctypes.c_size_t], _I),
     "se_world_set_light_field": ([_P, _P, ctypes.c_size_t], _I),
     "se_world_render_color": ([_P, _P, ctypes.c_size_t], _I),
+    "se_world_render_color_device": ([_P, ctypes.POINTER(_P)], _I),
     "se_world_create_band": ([_P, _I, _I, _I, _I, _I, ctypes.POINTER(_P)], _I),
     "se_world_band_info": ([_P] + [ctypes.POINTER(_I)] * 4, _I),
     "se_world_copy_rows": ([_P, _I, _I, _P, _I], _I),

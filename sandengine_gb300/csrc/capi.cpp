@@ -263,6 +263,16 @@ SE_API int se_world_render_color(se_world* w, float* rgba, size_t n_floats) {
   });
 }
 
+SE_API int se_world_render_color_device(se_world* w, float** rgba) {
+  return guard([&] {
+    if (!w || !rgba) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    se::rt::Status s = w->w->render_color();
+    if (!s.ok()) return ret(s);
+    *rgba = reinterpret_cast<float*>(w->w->d_color);
+    return (int)SE_OK;
+  });
+}
+
 SE_API int se_world_create(se_ruleset* rs, int width, int height, se_world** out) {
   return guard([&] {
     if (!rs || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
@@ -428,7 +438,7 @@ SE_API int se_world_set_timing(se_world* w, int enable) {
   return guard([&] {
     if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
     w->w->timing = enable != 0;
-    w->w->timed_used = 0;
+    for (auto& u : w->w->timed_used) u = 0;
     return (int)SE_OK;
   });
 }
@@ -437,7 +447,16 @@ SE_API int se_world_read_timing(se_world* w, double* kernel_ms, long long* launc
                                 long long* cells) {
   return guard([&] {
     if (!w || !kernel_ms || !launches || !cell_frames || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
-    return ret(w->w->timing_read(kernel_ms, launches, cell_frames, cells));
+    return ret(w->w->timing_read(0, kernel_ms, launches, cell_frames, cells));
+  });
+}
+
+SE_API int se_world_read_pass_timing(se_world* w, int pass, double* kernel_ms, long long* launches,
+                                     long long* cells) {
+  return guard([&] {
+    if (!w || !kernel_ms || !launches || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    long long cf = 0;
+    return ret(w->w->timing_read(pass, kernel_ms, launches, &cf, cells));
   });
 }
 

@@ -89,59 +89,108 @@ __global__ void __launch_bounds__(256) se_color_kernel(const uint32_t* __restric
   }
 }
 
+// Light pass over a 64 x 16 tile per CTA.  The tile plus a one-cell ring is staged in
+// shared memory as each cell's contribution to its neighbours' blend,
+// (rgb * keep * a, a) for its previous light (rgb, a), where keep is 0 when its old cell is a
+// light obstacle, else 1; plus a byte that marks cells outside the world.
+// Thread t computes the cells (t % 64, t / 64 + 4 j), j < 4: a warp touches 32 consecutive
+// cells of a row, so shared-memory reads and global loads / stores are contiguous.
+constexpr int LTW = 64, LTH = 16, LSW = LTW + 2, LSH = LTH + 2;
+
+// The 8-neighbour blend for the staged cell s0.  INTERIOR: all 8 neighbours lie in the
+// world (no checks; the mean's division by 8 is the product by 0.125, the same correctly
+// rounded quotient).
+template <bool INTERIOR>
+__device__ __forceinline__ float4 light_blend(const float4* sl, const uint8_t* sk, int s0) {
+  // neighbours in getDiagonalNeighbours order: DOWN, UP, DOWNLEFT, UPLEFT, DOWNRIGHT,
+  // UPRIGHT, RIGHT, LEFT (offsets in the staged array)
+  constexpr int NOFF[8] = {LSW, -LSW, LSW - 1, -LSW - 1, LSW + 1, -LSW + 1, 1, -1};
+  float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f, m0 = 0.0f, m1 = 0.0f, m2 = 0.0f, maxf = 0.0f;
+  int num = 0;
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const int s = s0 + NOFF[n];
+    if (!INTERIOR && sk[s]) continue;  // outside the world
+    const float4 c = sl[s];
+    const float t0 = c.x, t1 = c.y, t2 = c.z, a = c.w;
+    const float falloff = a == 0.0f ? maxf : a;
+    a0 = fadd(a0, t0);
+    a1 = fadd(a1, t1);
+    a2 = fadd(a2, t2);
+    a3 = fadd(a3, falloff);
+    maxf = gmax(falloff, maxf);
+    ++num;
+    m0 = gmax(m0, t0);  // the alpha of the maximum is not used (mix takes .rgb)
+    m1 = gmax(m1, t1);
+    m2 = gmax(m2, t2);
+  }
+  if (INTERIOR) {
+    a0 = fmul(a0, 0.125f);
+    a1 = fmul(a1, 0.125f);
+    a2 = fmul(a2, 0.125f);
+    a3 = fmul(a3, 0.125f);
+  } else if (num > 0) {
+    const float fn = (float)num;
+    a0 = __fdiv_rn(a0, fn);
+    a1 = __fdiv_rn(a1, fn);
+    a2 = __fdiv_rn(a2, fn);
+    a3 = __fdiv_rn(a3, fn);
+  }
+  // mix(avg.rgb, max.rgb, 0.5) = avg * (1 - 0.5) + max * 0.5
+  return make_float4(fadd(fmul(a0, 0.5f), fmul(m0, 0.5f)), fadd(fmul(a1, 0.5f), fmul(m1, 0.5f)),
+                     fadd(fmul(a2, 0.5f), fmul(m2, 0.5f)), a3);
+}
+
 __global__ void __launch_bounds__(256) se_light_kernel(const uint32_t* __restrict__ old_grid,
                                                        const uint32_t* __restrict__ new_grid,
                                                        const float4* __restrict__ lin, float4* __restrict__ lout,
                                                        int W, int H, const RenderMat* __restrict__ mats, int nmat) {
-  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
-  if (x >= W || y >= H) return;
-  const size_t i = (size_t)y * W + x;
-  const RenderMat* nm = mats + mat_index(__ldg(new_grid + i), nmat);
-  float4 L;
-  if (__ldg(&nm->flags) & kRenderEmits) {
-    L = make_float4(__ldg(nm->emission + 0), __ldg(nm->emission + 1), __ldg(nm->emission + 2),
-                    __ldg(nm->emission + 3));
-  } else if (y == 0) {
-    L = make_float4(1.0f, 1.0f, 1.0f, 0.999999f);
-  } else {
-    // neighbours in getDiagonalNeighbours order: DOWN, UP, DOWNLEFT, UPLEFT, DOWNRIGHT,
-    // UPRIGHT, RIGHT, LEFT
-    const int dx[8] = {0, 0, -1, -1, 1, 1, 1, -1}, dy[8] = {1, -1, 1, -1, 1, -1, 0, 0};
-    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f, m0 = 0.0f, m1 = 0.0f, m2 = 0.0f, maxf = 0.0f;
-    int num = 0;
-#pragma unroll
-    for (int n = 0; n < 8; ++n) {
-      const int qx = x + dx[n], qy = y + dy[n];
-      if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
-      const size_t q = (size_t)qy * W + qx;
-      const uint32_t om = mat_index(__ldg(old_grid + q), nmat);
-      const float keep = (__ldg(&mats[om].flags) & kRenderObstacle) ? 0.0f : 1.0f;
+  __shared__ float4 sl[LSH * LSW];  // contribution (rgb * keep * a, a) per staged cell
+  __shared__ uint8_t sk[LSH * LSW];  // 1: outside the world
+  __shared__ uint32_t sflags[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) sflags[i] = __ldg(&mats[mat_index((uint32_t)i, nmat)].flags);
+  __syncthreads();
+  const int X0 = blockIdx.x * LTW, Y0 = blockIdx.y * LTH;
+  for (int i = threadIdx.x; i < LSW * LSH; i += blockDim.x) {
+    const int r = i / LSW, c = i - r * LSW;
+    const int gx = X0 - 1 + c, gy = Y0 - 1 + r;
+    if (gx >= 0 && gy >= 0 && gx < W && gy < H) {
+      const size_t q = (size_t)gy * W + gx;
+      const uint32_t id = __ldg(old_grid + q);
+      const uint32_t fl = id < 256u ? sflags[id] : __ldg(&mats[mat_index(id, nmat)].flags);
+      const float keep = (fl & kRenderObstacle) ? 0.0f : 1.0f;
       const float4 l = __ldg(lin + q);
-      const float r = fmul(l.x, keep), g = fmul(l.y, keep), b = fmul(l.z, keep), a = fmul(l.w, 1.0f);
-      const float falloff = a == 0.0f ? maxf : a;
-      const float t0 = fmul(r, a), t1 = fmul(g, a), t2 = fmul(b, a), t3 = falloff;
-      a0 = fadd(a0, t0);
-      a1 = fadd(a1, t1);
-      a2 = fadd(a2, t2);
-      a3 = fadd(a3, t3);
-      maxf = gmax(falloff, maxf);
-      ++num;
-      m0 = gmax(m0, t0);
-      m1 = gmax(m1, t1);
-      m2 = gmax(m2, t2);  // the alpha of the maximum is not used (mix takes .rgb)
+      // light_data = light * vec4(vec3(keep), 1.0); contribution = (light_data.rgb * a, a)
+      sl[i] = make_float4(fmul(fmul(l.x, keep), l.w), fmul(fmul(l.y, keep), l.w), fmul(fmul(l.z, keep), l.w), l.w);
+      sk[i] = 0;
+    } else {
+      sk[i] = 1;
+      sl[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    if (num > 0) {
-      const float fn = (float)num;
-      a0 = __fdiv_rn(a0, fn);
-      a1 = __fdiv_rn(a1, fn);
-      a2 = __fdiv_rn(a2, fn);
-      a3 = __fdiv_rn(a3, fn);
-    }
-    // mix(avg.rgb, max.rgb, 0.5) = avg * (1 - 0.5) + max * 0.5
-    L = make_float4(fadd(fmul(a0, 0.5f), fmul(m0, 0.5f)), fadd(fmul(a1, 0.5f), fmul(m1, 0.5f)),
-                    fadd(fmul(a2, 0.5f), fmul(m2, 0.5f)), a3);
   }
-  lout[i] = L;
+  __syncthreads();
+  const bool interior = X0 >= 1 && Y0 >= 1 && X0 + LTW + 1 <= W && Y0 + LTH + 1 <= H;
+  const int cx = threadIdx.x & 63;
+  for (int j = 0; j < 4; ++j) {
+    const int cy = (threadIdx.x >> 6) + 4 * j;
+    const int x = X0 + cx, y = Y0 + cy;
+    if (x >= W || y >= H) continue;
+    const size_t i = (size_t)y * W + x;
+    const uint32_t nid = __ldg(new_grid + i);
+    const uint32_t nfl = nid < 256u ? sflags[nid] : __ldg(&mats[mat_index(nid, nmat)].flags);
+    float4 L;
+    if (nfl & kRenderEmits) {
+      const RenderMat* nm = mats + mat_index(nid, nmat);
+      L = make_float4(__ldg(nm->emission + 0), __ldg(nm->emission + 1), __ldg(nm->emission + 2),
+                      __ldg(nm->emission + 3));
+    } else if (y == 0) {
+      L = make_float4(1.0f, 1.0f, 1.0f, 0.999999f);
+    } else {
+      const int s0 = (cy + 1) * LSW + cx + 1;
+      L = interior ? light_blend<true>(sl, sk, s0) : light_blend<false>(sl, sk, s0);
+    }
+    lout[i] = L;
+  }
 }
 
 }  // namespace
@@ -165,7 +214,7 @@ cudaError_t render_color(const uint32_t* grid, const float* noise, float4* out, 
 
 cudaError_t light_pass(const uint32_t* old_grid, const uint32_t* new_grid, const float4* light_in, float4* light_out,
                        int W, int H, const RenderMat* mats, int nmat, cudaStream_t s) {
-  dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
+  dim3 grid((unsigned)((W + LTW - 1) / LTW), (unsigned)((H + LTH - 1) / LTH));
   se_light_kernel<<<grid, 256, 0, s>>>(old_grid, new_grid, light_in, light_out, W, H, mats, nmat);
   return cudaGetLastError();
 }

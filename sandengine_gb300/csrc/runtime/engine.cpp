@@ -77,10 +77,11 @@ Ruleset::~Ruleset() {
 }
 
 World::~World() {
-  for (auto& t : timed) {
-    cudaEventDestroy(t.a);
-    cudaEventDestroy(t.b);
-  }
+  for (auto& set : timed)
+    for (auto& t : set) {
+      cudaEventDestroy(t.a);
+      cudaEventDestroy(t.b);
+    }
   if (buf[0]) cudaFree(buf[0]);
   if (buf[1]) cudaFree(buf[1]);
   for (auto* l : light)
@@ -193,16 +194,8 @@ Status World::launch_tiles(int f0, int k, const TileVariant* v, bool commit) {
   if (!v || v->kmax < k) return {SE_ERR_INVALID_ARGUMENT, "no kernel variant for this many frames per launch"};
   Timed* t = nullptr;
   if (timing) {
-    if (timed_used == timed.size()) {
-      Timed n{};
-      SE_CUDA(cudaEventCreate(&n.a));
-      SE_CUDA(cudaEventCreate(&n.b));
-      timed.push_back(n);
-    }
-    t = &timed[timed_used++];
-    t->cells = (long long)W * H;
-    t->frames = k;
-    SE_CUDA(cudaEventRecord(t->a, stream));
+    Status s = timing_begin(0, (long long)W * H, k, &t);
+    if (!s.ok()) return s;
   }
   Status s = launch_tile_kernel(*rs, *v, buf[cur], buf[cur ^ 1], W, wh, f0, k, ya, ya + H, stream);
   if (!s.ok()) return s;
@@ -211,22 +204,40 @@ Status World::launch_tiles(int f0, int k, const TileVariant* v, bool commit) {
   return Status::Ok();
 }
 
-Status World::timing_read(double* ms, long long* launches, long long* cell_frames, long long* cells) {
+Status World::timing_begin(int pass, long long cells, int frames, Timed** out) {
+  auto& set = timed[pass];
+  if (timed_used[pass] == set.size()) {
+    Timed n{};
+    SE_CUDA(cudaEventCreate(&n.a));
+    SE_CUDA(cudaEventCreate(&n.b));
+    set.push_back(n);
+  }
+  Timed* t = &set[timed_used[pass]++];
+  t->cells = cells;
+  t->frames = frames;
+  SE_CUDA(cudaEventRecord(t->a, stream));
+  *out = t;
+  return Status::Ok();
+}
+
+Status World::timing_read(int pass, double* ms, long long* launches, long long* cell_frames, long long* cells) {
+  if (pass < 0 || pass > 2) return {SE_ERR_INVALID_ARGUMENT, "pass must be 0 (tiles), 1 (light) or 2 (colour)"};
   SE_CUDA(cudaStreamSynchronize(stream));
   double tot = 0;
   long long cf = 0, c = 0;
-  for (size_t i = 0; i < timed_used; ++i) {
+  const auto& set = timed[pass];
+  for (size_t i = 0; i < timed_used[pass]; ++i) {
     float m = 0;
-    SE_CUDA(cudaEventElapsedTime(&m, timed[i].a, timed[i].b));
+    SE_CUDA(cudaEventElapsedTime(&m, set[i].a, set[i].b));
     tot += m;
-    cf += timed[i].cells * timed[i].frames;
-    c += timed[i].cells;
+    cf += set[i].cells * set[i].frames;
+    c += set[i].cells;
   }
   *ms = tot;
-  *launches = (long long)timed_used;
+  *launches = (long long)timed_used[pass];
   *cell_frames = cf;
   *cells = c;
-  timed_used = 0;
+  timed_used[pass] = 0;
   return Status::Ok();
 }
 
@@ -373,8 +384,14 @@ Status World::set_light(bool on) {
 }
 
 Status World::light_frame() {
+  Timed* t = nullptr;
+  if (timing) {
+    Status s = timing_begin(1, (long long)W * H, 1, &t);
+    if (!s.ok()) return s;
+  }
   SE_CUDA(light_pass(buf[cur ^ 1], buf[cur], light[lcur], light[lcur ^ 1], W, H, rs->d_render,
                      rs->num_materials(), stream));
+  if (t) SE_CUDA(cudaEventRecord(t->b, stream));
   lcur ^= 1;
   return Status::Ok();
 }
@@ -390,7 +407,13 @@ Status World::render_color() {
     cudaError_t e = cudaMalloc(&d_color, (size_t)W * H * sizeof(float4));
     if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
   }
+  Timed* t = nullptr;
+  if (timing) {
+    Status s = timing_begin(2, (long long)W * H, 1, &t);
+    if (!s.ok()) return s;
+  }
   SE_CUDA(se::rt::render_color(buf[cur], d_noise, d_color, W, H, rs->d_render, rs->num_materials(), stream));
+  if (t) SE_CUDA(cudaEventRecord(t->b, stream));
   return Status::Ok();
 }
 

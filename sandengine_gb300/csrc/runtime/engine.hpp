@@ -83,16 +83,18 @@ struct World {
   Status autotune(int reps, int* best_k);
   Status launch_edit(const se_modification* mods, int nlive);
   int default_k() const;
-  // Opt-in per-launch CUDA-event timing of the tile kernel (for roofline measurements).
+  // Opt-in per-launch CUDA-event timing (for roofline measurements) of the tile kernel
+  // (pass 0), the light pass (1) and the colour pass (2).
   bool timing = false;
   struct Timed {
     cudaEvent_t a, b;
-    long long cells;  // W*H of the launch
+    long long cells;  // cells the launch covered
     int frames;       // frames the launch advanced
   };
-  std::vector<Timed> timed;
-  size_t timed_used = 0;
-  Status timing_read(double* ms, long long* launches, long long* cell_frames, long long* cells);
+  std::vector<Timed> timed[3];
+  size_t timed_used[3] = {0, 0, 0};
+  Status timing_begin(int pass, long long cells, int frames, Timed** out);
+  Status timing_read(int pass, double* ms, long long* launches, long long* cell_frames, long long* cells);
   Status digest(unsigned long long* out);
   Status histogram(unsigned long long* counts, int nbins);
 

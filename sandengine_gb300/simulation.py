@@ -184,6 +184,21 @@ class Simulation:
         check(lib().se_world_render_color(self._h, out.ctypes.data, out.size))
         return out
 
+    def render_color_device(self) -> int:
+        """Render output_color into the world's device buffer (stream-ordered); returns its
+        address (RGBA32F, height x width x 4)."""
+        p = ctypes.c_void_p()
+        check(lib().se_world_render_color_device(self._h, ctypes.byref(p)))
+        return p.value or 0
+
+    def read_pass_timing(self, pass_: int) -> dict:
+        """Kernel time, launches and cells of the light (1) or colour (2) passes since the
+        last read (synchronizes)."""
+        ms, n, c = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_longlong()
+        check(lib().se_world_read_pass_timing(self._h, int(pass_), ctypes.byref(ms), ctypes.byref(n),
+                                              ctypes.byref(c)))
+        return {"kernel_ms": ms.value, "launches": n.value, "cells": c.value}
+
     def digest(self) -> int:
         d = ctypes.c_uint64(0)
         check(lib().se_world_digest(self._h, ctypes.byref(d)))
