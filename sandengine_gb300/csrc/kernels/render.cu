@@ -145,42 +145,59 @@ __global__ void __launch_bounds__(256) se_light_kernel(const uint32_t* __restric
                                                        const uint32_t* __restrict__ new_grid,
                                                        const float4* __restrict__ lin, float4* __restrict__ lout,
                                                        int W, int H, const RenderMat* __restrict__ mats, int nmat) {
-  __shared__ float4 sl[LSH * LSW];  // contribution (rgb * keep * a, a) per staged cell
-  __shared__ uint8_t sk[LSH * LSW];  // 1: outside the world
-  __shared__ uint32_t sflags[256];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) sflags[i] = __ldg(&mats[mat_index((uint32_t)i, nmat)].flags);
-  __syncthreads();
+  constexpr int NT = 256, NS = LSW * LSH, NU = (NS + NT - 1) / NT;
+  __shared__ float4 sl[NS];  // contribution (rgb * keep * a, a) per staged cell
+  __shared__ uint8_t sk[NS];  // 1: outside the world
   const int X0 = blockIdx.x * LTW, Y0 = blockIdx.y * LTH;
-  for (int i = threadIdx.x; i < LSW * LSH; i += blockDim.x) {
+  // Issue every global load of this thread first (staged ids and light, then the new ids
+  // of its four cells), so that they are in flight together.
+  uint32_t ids[NU];
+  float4 ls[NU];
+  bool in[NU];
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    const int i = threadIdx.x + u * NT;
     const int r = i / LSW, c = i - r * LSW;
     const int gx = X0 - 1 + c, gy = Y0 - 1 + r;
-    if (gx >= 0 && gy >= 0 && gx < W && gy < H) {
+    in[u] = i < NS && gx >= 0 && gy >= 0 && gx < W && gy < H;
+    if (in[u]) {
       const size_t q = (size_t)gy * W + gx;
-      const uint32_t id = __ldg(old_grid + q);
-      const uint32_t fl = id < 256u ? sflags[id] : __ldg(&mats[mat_index(id, nmat)].flags);
-      const float keep = (fl & kRenderObstacle) ? 0.0f : 1.0f;
-      const float4 l = __ldg(lin + q);
+      ids[u] = __ldg(old_grid + q);
+      ls[u] = __ldg(lin + q);
+    }
+  }
+  const int cx = threadIdx.x & 63;
+  uint32_t nid[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int x = X0 + cx, y = Y0 + (threadIdx.x >> 6) + 4 * j;
+    nid[j] = (x < W && y < H) ? __ldg(new_grid + (size_t)y * W + x) : 0u;
+  }
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    const int i = threadIdx.x + u * NT;
+    if (i >= NS) break;
+    if (in[u]) {
+      const float keep = (__ldg(&mats[mat_index(ids[u], nmat)].flags) & kRenderObstacle) ? 0.0f : 1.0f;
+      const float4 l = ls[u];
       // light_data = light * vec4(vec3(keep), 1.0); contribution = (light_data.rgb * a, a)
       sl[i] = make_float4(fmul(fmul(l.x, keep), l.w), fmul(fmul(l.y, keep), l.w), fmul(fmul(l.z, keep), l.w), l.w);
       sk[i] = 0;
     } else {
-      sk[i] = 1;
       sl[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      sk[i] = 1;
     }
   }
   __syncthreads();
   const bool interior = X0 >= 1 && Y0 >= 1 && X0 + LTW + 1 <= W && Y0 + LTH + 1 <= H;
-  const int cx = threadIdx.x & 63;
+#pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int cy = (threadIdx.x >> 6) + 4 * j;
     const int x = X0 + cx, y = Y0 + cy;
     if (x >= W || y >= H) continue;
-    const size_t i = (size_t)y * W + x;
-    const uint32_t nid = __ldg(new_grid + i);
-    const uint32_t nfl = nid < 256u ? sflags[nid] : __ldg(&mats[mat_index(nid, nmat)].flags);
+    const RenderMat* nm = mats + mat_index(nid[j], nmat);
     float4 L;
-    if (nfl & kRenderEmits) {
-      const RenderMat* nm = mats + mat_index(nid, nmat);
+    if (__ldg(&nm->flags) & kRenderEmits) {
       L = make_float4(__ldg(nm->emission + 0), __ldg(nm->emission + 1), __ldg(nm->emission + 2),
                       __ldg(nm->emission + 3));
     } else if (y == 0) {
@@ -189,7 +206,7 @@ __global__ void __launch_bounds__(256) se_light_kernel(const uint32_t* __restric
       const int s0 = (cy + 1) * LSW + cx + 1;
       L = interior ? light_blend<true>(sl, sk, s0) : light_blend<false>(sl, sk, s0);
     }
-    lout[i] = L;
+    lout[(size_t)y * W + x] = L;
   }
 }
 
