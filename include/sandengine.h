@@ -127,6 +127,18 @@ int se_world_render_color(se_world* w, float* rgba, size_t n_floats);
  * synchronization); *rgba stays valid until the next render or se_world_destroy. */
 int se_world_render_color_device(se_world* w, float** rgba);
 
+/* Headless composite of the current grid (shaders/fragment140.glsl:70-100, drawn by
+ * renderer.rs:212-246 as a full-screen quad): one RGBA32F pixel per cell, rows top to
+ * bottom.  The colour field's box-filter mip pyramid gives the three blurred-alpha
+ * occlusion terms; the light field is used when kept (else zero light); bg_rgba is an
+ * optional bg_w x bg_h RGBA32F background (host or device memory; NULL: transparent).
+ * GL filtering is fixed to the spec's formulas in binary32: mirrored-repeat wrap,
+ * nearest / bilinear taps, LINEAR_MIPMAP_NEAREST level choice. */
+int se_world_composite(se_world* w, const float* bg_rgba, int bg_w, int bg_h, float* out_rgba, size_t n_floats);
+/* The same into the world's own device buffer, stream-ordered; *out_rgba stays valid until
+ * the next composite or se_world_destroy. */
+int se_world_composite_device(se_world* w, const float* bg_rgba, int bg_w, int bg_h, float** out_rgba);
+
 /* ---- row bands of one world (no counterpart in the reference, which runs one world on
  * one GPU) ------------------------------------------------------------------------------
  * A band world holds rows [row0, row0 + rows) of a width x world_height world plus up to
@@ -212,7 +224,8 @@ int se_world_set_timing(se_world* w, int enable);
 int se_world_read_timing(se_world* w, double* kernel_ms, long long* launches, long long* cell_frames,
                          long long* cells);
 /* The same for the light pass (pass = 1; algorithmic bytes 40 x cells: old and new id, old
- * and new RGBA32F light) and the colour pass (pass = 2; 24 x cells: id, noise, RGBA32F). */
+ * and new RGBA32F light), the colour pass (pass = 2; 24 x cells: id, noise, RGBA32F) and the
+ * composite (pass = 3; 48 x cells: colour, light, output; its pyramid is not timed). */
 int se_world_read_pass_timing(se_world* w, int pass, double* kernel_ms, long long* launches, long long* cells);
 
 /* ---- many worlds (no counterpart in the reference, which runs one world) --------------- */

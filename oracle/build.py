@@ -144,6 +144,9 @@ class Port:
         self.lib.port_hash43.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         self.lib.port_color.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         self.lib.port_light.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int]
+        self.lib.port_mip_level.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        self.lib.port_composite.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] + [ctypes.c_void_p] * 2 + \
+            [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 2
         self.num_materials = self.lib.port_num_materials()
 
     def color(self, grid: np.ndarray) -> np.ndarray:
@@ -151,6 +154,34 @@ class Port:
         g = np.ascontiguousarray(grid, dtype=np.uint32)
         out = np.empty(g.shape + (4,), dtype=np.float32)
         self.lib.port_color(g.ctypes.data, g.shape[1], g.shape[0], out.ctypes.data)
+        return out
+
+    def mips(self, color: np.ndarray):
+        """The box-filter pyramid of an (H, W, 4) float32 field, level 0 first."""
+        levels = [np.ascontiguousarray(color, dtype=np.float32)]
+        while levels[-1].shape[0] > 1 or levels[-1].shape[1] > 1:
+            h, w = levels[-1].shape[:2]
+            nxt = np.empty((max(1, h // 2), max(1, w // 2), 4), dtype=np.float32)
+            self.lib.port_mip_level(levels[-1].ctypes.data, w, h, nxt.ctypes.data)
+            levels.append(nxt)
+        return levels
+
+    # exp(-gamma) for gamma 0.5, 0.35, 0.2, rounded to binary32 (the library's constants)
+    BLUR_SIDE = np.array([0.606530666, 0.704688072, 0.818730772], dtype=np.float32)
+
+    def composite(self, color: np.ndarray, light=None, background=None) -> np.ndarray:
+        """fragment140.glsl over a colour field (and its pyramid), an optional light field and
+        an optional background image: (H, W, 4) float32."""
+        levels = self.mips(color)
+        ptrs = (ctypes.c_void_p * len(levels))(*[lv.ctypes.data for lv in levels])
+        lw = (ctypes.c_int * len(levels))(*[lv.shape[1] for lv in levels])
+        lh = (ctypes.c_int * len(levels))(*[lv.shape[0] for lv in levels])
+        li = None if light is None else np.ascontiguousarray(light, dtype=np.float32)
+        bg = None if background is None else np.ascontiguousarray(background, dtype=np.float32)
+        out = np.empty(levels[0].shape, dtype=np.float32)
+        self.lib.port_composite(ptrs, lw, lh, len(levels), None if li is None else li.ctypes.data,
+                                None if bg is None else bg.ctypes.data, 0 if bg is None else bg.shape[1],
+                                0 if bg is None else bg.shape[0], self.BLUR_SIDE.ctypes.data, out.ctypes.data)
         return out
 
     def light(self, old: np.ndarray, new: np.ndarray, light_in: np.ndarray) -> np.ndarray:

@@ -23,6 +23,7 @@
 // the value main() stores for it.
 #include <cstdint>
 #include <cstring>
+#include <vector>
 
 #include "glsl_shim.hpp"
 
@@ -389,6 +390,136 @@ SE_EXPORT void port_light(const uint32_t* old_grid, const uint32_t* new_grid, co
       }
       float* o = lout + 4 * ((int64_t)y * W + x);
       for (int c = 0; c < 4; ++c) o[c] = L[c];
+    }
+}
+
+// ---- headless composite (shaders/fragment140.glsl:70-100) ----------------------------------
+// One output pixel per texel (the full-screen quad of renderer.rs:212-246 at the grid's
+// size), texel rows top to bottom, so the fragment at column c, row r samples
+// uv = ((c + 0.5) / W, (r + 0.5) / H) (vertex140.glsl flips v, the window origin is at the
+// bottom).  GL's texture filtering and mipmap generation are left to the driver; this
+// restatement fixes them to the spec's formulas in binary32: mirrored-repeat wrap,
+// nearest and bilinear taps, LINEAR_MIPMAP_NEAREST level choice (level ceil(lod + 0.5) - 1
+// for lod > 0.5, the magnification filter for lod <= 0), a 2x2 box-filter pyramid with the
+// last row / column repeated for odd sizes, pow(x, 2.0) = x * x.  The blur weights
+// exp(-gamma) arrive precomputed (w[0..2] for gamma 0.5, 0.35, 0.2).
+
+}  // extern "C"
+namespace {
+
+struct Level {
+  const float* t;  // RGBA
+  int w, h;
+};
+
+inline int mirror(int i, int n) {  // GL_MIRRORED_REPEAT on texel indices
+  const int p = 2 * n;
+  int m = i % p;
+  if (m < 0) m += p;
+  return m >= n ? p - 1 - m : m;
+}
+
+inline void texel(const Level& L, int i, int j, float o[4]) {
+  const float* p = L.t + 4 * ((int64_t)mirror(j, L.h) * L.w + mirror(i, L.w));
+  for (int c = 0; c < 4; ++c) o[c] = p[c];
+}
+
+inline void sample_nearest(const Level& L, float u, float v, float o[4]) {
+  texel(L, (int)floor(u * (float)L.w), (int)floor(v * (float)L.h), o);
+}
+
+inline void sample_linear(const Level& L, float u, float v, float o[4]) {
+  const float x = u * (float)L.w - 0.5f, y = v * (float)L.h - 0.5f;
+  const float fx = floor(x), fy = floor(y);
+  const float a = x - fx, b = y - fy;
+  const int i = (int)fx, j = (int)fy;
+  float t00[4], t10[4], t01[4], t11[4];
+  texel(L, i, j, t00);
+  texel(L, i + 1, j, t10);
+  texel(L, i, j + 1, t01);
+  texel(L, i + 1, j + 1, t11);
+  const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+  for (int c = 0; c < 4; ++c) o[c] = ((t00[c] * w00 + t10[c] * w10) + t01[c] * w01) + t11[c] * w11;
+}
+
+// textureLod with MAG NEAREST / MIN LINEAR_MIPMAP_NEAREST
+inline void sample_lod(const std::vector<Level>& mips, float u, float v, float lod, float o[4]) {
+  if (lod <= 0.0f) return sample_nearest(mips[0], u, v, o);
+  int d = lod <= 0.5f ? 0 : (int)__builtin_ceilf(lod + 0.5f) - 1;
+  if (d > (int)mips.size() - 1) d = (int)mips.size() - 1;
+  sample_linear(mips[(size_t)d], u, v, o);
+}
+
+// fragment140.glsl:37-50 sampleBlurred(tex, uv, radius, gamma), alpha only (the only
+// channel main() reads); lod = log2(radius) is exact for 2, 16, 32.
+inline float blurred_alpha(const std::vector<Level>& mips, float u, float v, float lod, float w_side) {
+  float acc = 0.0f, wsum = 0.0f;
+  for (int k = -1; k <= 1; ++k) {
+    const float i = lod + (float)k;
+    const float w = k == 0 ? 1.0f : w_side;  // exp(-gamma * pow(lod - i, 2))
+    float t[4];
+    sample_lod(mips, u, v, i, t);
+    acc = acc + t[3] * w;
+    wsum = wsum + w;
+  }
+  return acc / wsum;
+}
+
+}  // namespace
+extern "C" {
+
+// The box-filter pyramid of an RGBA level: out (w/2 or 1) x (h/2 or 1), each texel the
+// mean of a 2x2 block (indices clamped to the source).
+SE_EXPORT void port_mip_level(const float* src, int sw, int sh, float* dst) {
+  const int dw = sw > 1 ? sw / 2 : 1, dh = sh > 1 ? sh / 2 : 1;
+  for (int y = 0; y < dh; ++y)
+    for (int x = 0; x < dw; ++x) {
+      const int x0 = 2 * x < sw ? 2 * x : sw - 1, x1 = 2 * x + 1 < sw ? 2 * x + 1 : sw - 1;
+      const int y0 = 2 * y < sh ? 2 * y : sh - 1, y1 = 2 * y + 1 < sh ? 2 * y + 1 : sh - 1;
+      for (int c = 0; c < 4; ++c) {
+        float s = src[4 * ((int64_t)y0 * sw + x0) + c] + src[4 * ((int64_t)y0 * sw + x1) + c];
+        s = s + src[4 * ((int64_t)y1 * sw + x0) + c];
+        s = s + src[4 * ((int64_t)y1 * sw + x1) + c];
+        dst[4 * ((int64_t)y * dw + x) + c] = s * 0.25f;
+      }
+    }
+}
+
+// fragment140.glsl:70-100 for every pixel.  color: the colour field with its pyramid
+// (levels[0] = color, as port_mip_level makes them, nlevels of them); light: the light
+// field (or null: zero light); bg: background RGBA of bw x bh (or null: transparent).
+SE_EXPORT void port_composite(const float* const* levels, const int* lw, const int* lh, int nlevels,
+                              const float* light, const float* bg, int bw, int bh, const float* w_side, float* out) {
+  std::vector<Level> mips;
+  for (int l = 0; l < nlevels; ++l) mips.push_back(Level{levels[l], lw[l], lh[l]});
+  const int W = lw[0], H = lh[0];
+  const Level lightL{light, W, H}, bgL{bg, bw, bh};
+  const float pixelate = (float)W / 2.0f;
+  const float d = 1.0f / pixelate;
+  for (int r = 0; r < H; ++r)
+    for (int cix = 0; cix < W; ++cix) {
+      const float u = ((float)cix + 0.5f) / (float)W, v = ((float)r + 0.5f) / (float)H;
+      const float pu = floor(u / d) * d, pv = floor(v / d) * d;
+      float col[4];
+      sample_nearest(mips[0], u, v, col);  // texture(color_tex, uv, 0.0): 1:1, magnification
+      float li[4] = {0, 0, 0, 0};
+      if (light) sample_linear(lightL, pu, pv, li);
+      for (int c = 0; c < 3; ++c) li[c] = clamp(li[c], 0.0f, 1.0f);
+      float occ = 1.0f - blurred_alpha(mips, pu, pv, 1.0f, w_side[0]);
+      const float occ2 = 1.0f - blurred_alpha(mips, pu, pv, 4.0f, w_side[1]);
+      const float occ3 = 1.0f - blurred_alpha(mips, pu, pv, 5.0f, w_side[2]);
+      occ = occ + (occ2 * 0.4f + occ3 * 0.25f);
+      occ = clamp(occ, 0.0f, 1.0f);
+      const float ambient = 0.1f;
+      const float sky = 0.5f * (1.0f - pv);
+      const float shade = ambient + occ * (1.0f - ambient);
+      for (int c = 0; c < 3; ++c) col[c] = clamp(col[c] * shade, 0.0f, 1.0f);
+      float b[4] = {0, 0, 0, 0};
+      if (bg) sample_linear(bgL, u, 1.0f - v, b);
+      float* o = out + 4 * ((int64_t)r * W + cix);
+      for (int c = 0; c < 4; ++c) o[c] = b[c] * (1.0f - col[3]) + col[c] * col[3];  // mix(bg, col, col.a)
+      for (int c = 0; c < 3; ++c) o[c] = o[c] * ((ambient + sky) + li[c]);
+      o[3] = o[3] * 1.0f;
     }
 }
 

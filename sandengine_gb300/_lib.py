@@ -64,6 +64,8 @@ _SIGS = {
     "se_world_set_light_field": ([_P, _P, ctypes.c_size_t], _I),
     "se_world_render_color": ([_P, _P, ctypes.c_size_t], _I),
     "se_world_render_color_device": ([_P, ctypes.POINTER(_P)], _I),
+    "se_world_composite": ([_P, _P, _I, _I, _P, ctypes.c_size_t], _I),
+    "se_world_composite_device": ([_P, _P, _I, _I, ctypes.POINTER(_P)], _I),
     "se_world_create_band": ([_P, _I, _I, _I, _I, _I, ctypes.POINTER(_P)], _I),
     "se_world_band_info": ([_P] + [ctypes.POINTER(_I)] * 4, _I),
     "se_world_copy_rows": ([_P, _I, _I, _P, _I], _I),

@@ -273,6 +273,32 @@ SE_API int se_world_render_color_device(se_world* w, float** rgba) {
   });
 }
 
+SE_API int se_world_composite(se_world* w, const float* bg_rgba, int bg_w, int bg_h, float* out_rgba,
+                              size_t n_floats) {
+  return guard([&] {
+    if (!w || !out_rgba) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    auto& W = *w->w;
+    const size_t need = (size_t)W.W * W.H * 4;
+    if (n_floats < need) return fail(SE_ERR_INVALID_ARGUMENT, "buffer smaller than width * height * 4 floats");
+    se::rt::Status s = W.composite(bg_rgba, bg_w, bg_h);
+    if (!s.ok()) return ret(s);
+    cudaError_t e = cudaMemcpyAsync(out_rgba, W.d_composite, need * 4, cudaMemcpyDefault, W.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(W.stream);
+    if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_world_composite_device(se_world* w, const float* bg_rgba, int bg_w, int bg_h, float** out_rgba) {
+  return guard([&] {
+    if (!w || !out_rgba) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    se::rt::Status s = w->w->composite(bg_rgba, bg_w, bg_h);
+    if (!s.ok()) return ret(s);
+    *out_rgba = reinterpret_cast<float*>(w->w->d_composite);
+    return (int)SE_OK;
+  });
+}
+
 SE_API int se_world_create(se_ruleset* rs, int width, int height, se_world** out) {
   return guard([&] {
     if (!rs || !out) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");

@@ -210,7 +210,120 @@ __global__ void __launch_bounds__(256) se_light_kernel(const uint32_t* __restric
   }
 }
 
+// ---- headless composite ---------------------------------------------------------------
+__device__ __forceinline__ int mirror_index(int i, int n) {  // GL_MIRRORED_REPEAT on texel indices
+  const int p = 2 * n;
+  int m = i % p;
+  if (m < 0) m += p;
+  return m >= n ? p - 1 - m : m;
+}
+__device__ __forceinline__ float4 tap(const float4* t, int w, int h, int i, int j) {
+  return __ldg(t + (size_t)mirror_index(j, h) * w + mirror_index(i, w));
+}
+__device__ __forceinline__ float4 sample_nearest(const float4* t, int w, int h, float u, float v) {
+  return tap(t, w, h, (int)floorf(fmul(u, (float)w)), (int)floorf(fmul(v, (float)h)));
+}
+__device__ __forceinline__ float lerp4(float t00, float t10, float t01, float t11, float w00, float w10, float w01,
+                                       float w11) {
+  return fadd(fadd(fadd(fmul(t00, w00), fmul(t10, w10)), fmul(t01, w01)), fmul(t11, w11));
+}
+__device__ float4 sample_linear(const float4* t, int w, int h, float u, float v) {
+  const float x = fsub(fmul(u, (float)w), 0.5f), y = fsub(fmul(v, (float)h), 0.5f);
+  const float fx = floorf(x), fy = floorf(y);
+  const float a = fsub(x, fx), b = fsub(y, fy);
+  const int i = (int)fx, j = (int)fy;
+  const float4 t00 = tap(t, w, h, i, j), t10 = tap(t, w, h, i + 1, j), t01 = tap(t, w, h, i, j + 1),
+               t11 = tap(t, w, h, i + 1, j + 1);
+  const float w00 = fmul(fsub(1.0f, a), fsub(1.0f, b)), w10 = fmul(a, fsub(1.0f, b)), w01 = fmul(fsub(1.0f, a), b),
+              w11 = fmul(a, b);
+  return make_float4(lerp4(t00.x, t10.x, t01.x, t11.x, w00, w10, w01, w11),
+                     lerp4(t00.y, t10.y, t01.y, t11.y, w00, w10, w01, w11),
+                     lerp4(t00.z, t10.z, t01.z, t11.z, w00, w10, w01, w11),
+                     lerp4(t00.w, t10.w, t01.w, t11.w, w00, w10, w01, w11));
+}
+// textureLod with MAG NEAREST / MIN LINEAR_MIPMAP_NEAREST, alpha only
+__device__ float sample_lod_alpha(const MipChain& m, float u, float v, float lod) {
+  if (lod <= 0.0f) return sample_nearest(m.level[0], m.w[0], m.h[0], u, v).w;
+  int d = lod <= 0.5f ? 0 : (int)ceilf(fadd(lod, 0.5f)) - 1;
+  if (d > m.n - 1) d = m.n - 1;
+  return sample_linear(m.level[d], m.w[d], m.h[d], u, v).w;
+}
+// sampleBlurred(tex, uv, radius, gamma).a with lod = log2(radius)
+__device__ float blurred_alpha(const MipChain& m, float u, float v, float lod, float w_side) {
+  float acc = 0.0f, wsum = 0.0f;
+#pragma unroll
+  for (int k = -1; k <= 1; ++k) {
+    const float w = k == 0 ? 1.0f : w_side;  // exp(-gamma * pow(lod - i, 2))
+    acc = fadd(acc, fmul(sample_lod_alpha(m, u, v, fadd(lod, (float)k)), w));
+    wsum = fadd(wsum, w);
+  }
+  return __fdiv_rn(acc, wsum);
+}
+
+__global__ void __launch_bounds__(256) se_mip_kernel(const float4* __restrict__ src, int sw, int sh,
+                                                     float4* __restrict__ dst, int dw, int dh) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (x >= dw || y >= dh) return;
+  const int x0 = min(2 * x, sw - 1), x1 = min(2 * x + 1, sw - 1), y0 = min(2 * y, sh - 1), y1 = min(2 * y + 1, sh - 1);
+  const float4 a = __ldg(src + (size_t)y0 * sw + x0), b = __ldg(src + (size_t)y0 * sw + x1),
+               c = __ldg(src + (size_t)y1 * sw + x0), d = __ldg(src + (size_t)y1 * sw + x1);
+  dst[(size_t)y * dw + x] = make_float4(fmul(fadd(fadd(fadd(a.x, b.x), c.x), d.x), 0.25f),
+                                        fmul(fadd(fadd(fadd(a.y, b.y), c.y), d.y), 0.25f),
+                                        fmul(fadd(fadd(fadd(a.z, b.z), c.z), d.z), 0.25f),
+                                        fmul(fadd(fadd(fadd(a.w, b.w), c.w), d.w), 0.25f));
+}
+
+__global__ void __launch_bounds__(256) se_composite_kernel(const MipChain m, const float4* __restrict__ light,
+                                                           const float4* __restrict__ bg, int bw, int bh, float ws0,
+                                                           float ws1, float ws2, float4* __restrict__ out) {
+  const int W = m.w[0], H = m.h[0];
+  const int cx = blockIdx.x * 32 + (threadIdx.x & 31), r = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (cx >= W || r >= H) return;
+  const float pixelate = __fdiv_rn((float)W, 2.0f);
+  const float d = __fdiv_rn(1.0f, pixelate);
+  const float u = __fdiv_rn(fadd((float)cx, 0.5f), (float)W), v = __fdiv_rn(fadd((float)r, 0.5f), (float)H);
+  const float pu = fmul(floorf(__fdiv_rn(u, d)), d), pv = fmul(floorf(__fdiv_rn(v, d)), d);
+  float4 col = sample_nearest(m.level[0], W, H, u, v);  // texture(color_tex, uv, 0.0): 1:1, magnification
+  float4 li = light ? sample_linear(light, W, H, pu, pv) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  li.x = gclamp(li.x, 0.0f, 1.0f);
+  li.y = gclamp(li.y, 0.0f, 1.0f);
+  li.z = gclamp(li.z, 0.0f, 1.0f);
+  float occ = fsub(1.0f, blurred_alpha(m, pu, pv, 1.0f, ws0));
+  const float occ2 = fsub(1.0f, blurred_alpha(m, pu, pv, 4.0f, ws1));
+  const float occ3 = fsub(1.0f, blurred_alpha(m, pu, pv, 5.0f, ws2));
+  occ = gclamp(fadd(occ, fadd(fmul(occ2, 0.4f), fmul(occ3, 0.25f))), 0.0f, 1.0f);
+  const float ambient = 0.1f;
+  const float sky = fmul(0.5f, fsub(1.0f, pv));
+  const float shade = fadd(ambient, fmul(occ, fsub(1.0f, ambient)));
+  col.x = gclamp(fmul(col.x, shade), 0.0f, 1.0f);
+  col.y = gclamp(fmul(col.y, shade), 0.0f, 1.0f);
+  col.z = gclamp(fmul(col.z, shade), 0.0f, 1.0f);
+  const float4 b = bg ? sample_linear(bg, bw, bh, u, fsub(1.0f, v)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float ia = fsub(1.0f, col.w);
+  const float base = fadd(ambient, sky);
+  float4 o;  // mix(bg, col, col.a) * vec4(ambient + sky + light, 1.0)
+  o.x = fmul(fadd(fmul(b.x, ia), fmul(col.x, col.w)), fadd(base, li.x));
+  o.y = fmul(fadd(fmul(b.y, ia), fmul(col.y, col.w)), fadd(base, li.y));
+  o.z = fmul(fadd(fmul(b.z, ia), fmul(col.z, col.w)), fadd(base, li.z));
+  o.w = fmul(fadd(fmul(b.w, ia), fmul(col.w, col.w)), 1.0f);
+  out[(size_t)r * W + cx] = o;
+}
+
 }  // namespace
+
+cudaError_t render_mip(const float4* src, int sw, int sh, float4* dst, cudaStream_t s) {
+  const int dw = mip_next(sw), dh = mip_next(sh);
+  dim3 grid((unsigned)((dw + 31) / 32), (unsigned)((dh + 7) / 8));
+  se_mip_kernel<<<grid, 256, 0, s>>>(src, sw, sh, dst, dw, dh);
+  return cudaGetLastError();
+}
+
+cudaError_t render_composite(const MipChain& mips, const float4* light, const float4* bg, int bw, int bh,
+                             const float w_side[3], float4* out, cudaStream_t s) {
+  dim3 grid((unsigned)((mips.w[0] + 31) / 32), (unsigned)((mips.h[0] + 7) / 8));
+  se_composite_kernel<<<grid, 256, 0, s>>>(mips, light, bg, bw, bh, w_side[0], w_side[1], w_side[2], out);
+  return cudaGetLastError();
+}
 
 cudaError_t render_noise(float* noise, int W, int H, cudaStream_t s) {
   dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));

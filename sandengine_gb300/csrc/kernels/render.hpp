@@ -31,4 +31,22 @@ cudaError_t render_color(const uint32_t* grid, const float* noise, float4* out, 
 cudaError_t light_pass(const uint32_t* old_grid, const uint32_t* new_grid, const float4* light_in, float4* light_out,
                        int W, int H, const RenderMat* mats, int nmat, cudaStream_t s);
 
+// Headless composite (shaders/fragment140.glsl:70-100): the colour field's box-filter
+// pyramid, then one RGBA32F pixel per texel.  GL filtering is fixed to the spec's formulas
+// in binary32 (mirrored-repeat wrap, nearest / bilinear taps, LINEAR_MIPMAP_NEAREST level
+// choice); the three blur weights exp(-gamma) for gamma 0.5, 0.35, 0.2 are passed in.
+constexpr int kMaxMipLevels = 24;
+struct MipChain {
+  const float4* level[kMaxMipLevels];
+  int w[kMaxMipLevels], h[kMaxMipLevels];
+  int n;
+};
+// exp(-gamma) for the three sampleBlurred calls (gamma 0.5, 0.35, 0.2), rounded to binary32.
+constexpr float kBlurSideWeight[3] = {0.606530666f, 0.704688072f, 0.818730772f};
+// Size of the next level: halved, at least 1.
+inline int mip_next(int n) { return n > 1 ? n / 2 : 1; }
+cudaError_t render_mip(const float4* src, int sw, int sh, float4* dst, cudaStream_t s);
+cudaError_t render_composite(const MipChain& mips, const float4* light, const float4* bg, int bw, int bh,
+                             const float w_side[3], float4* out, cudaStream_t s);
+
 }  // namespace se::rt

@@ -88,6 +88,9 @@ World::~World() {
     if (l) cudaFree(l);
   if (d_noise) cudaFree(d_noise);
   if (d_color) cudaFree(d_color);
+  for (auto* m : mips) cudaFree(m);
+  if (d_composite) cudaFree(d_composite);
+  if (d_bg) cudaFree(d_bg);
   if (d_scratch) cudaFree(d_scratch);
   if (own_stream) cudaStreamDestroy(own_stream);
 }
@@ -221,7 +224,8 @@ Status World::timing_begin(int pass, long long cells, int frames, Timed** out) {
 }
 
 Status World::timing_read(int pass, double* ms, long long* launches, long long* cell_frames, long long* cells) {
-  if (pass < 0 || pass > 2) return {SE_ERR_INVALID_ARGUMENT, "pass must be 0 (tiles), 1 (light) or 2 (colour)"};
+  if (pass < 0 || pass > 3)
+    return {SE_ERR_INVALID_ARGUMENT, "pass must be 0 (tiles), 1 (light), 2 (colour) or 3 (composite)"};
   SE_CUDA(cudaStreamSynchronize(stream));
   double tot = 0;
   long long cf = 0, c = 0;
@@ -413,6 +417,60 @@ Status World::render_color() {
     if (!s.ok()) return s;
   }
   SE_CUDA(se::rt::render_color(buf[cur], d_noise, d_color, W, H, rs->d_render, rs->num_materials(), stream));
+  if (t) SE_CUDA(cudaEventRecord(t->b, stream));
+  return Status::Ok();
+}
+
+Status World::composite(const float* bg, int bw, int bh) {
+  if (bg && (bw <= 0 || bh <= 0)) return {SE_ERR_INVALID_ARGUMENT, "background size must be positive"};
+  Status s = render_color();
+  if (!s.ok()) return s;
+  MipChain chain{};
+  chain.level[0] = d_color;
+  chain.w[0] = W;
+  chain.h[0] = H;
+  chain.n = 1;
+  for (int w = W, h = H; (w > 1 || h > 1) && chain.n < kMaxMipLevels; ++chain.n) {
+    const int nw = mip_next(w), nh = mip_next(h);
+    if ((int)mips.size() < chain.n) {
+      float4* m = nullptr;
+      cudaError_t e = cudaMalloc(&m, (size_t)nw * nh * sizeof(float4));
+      if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+      mips.push_back(m);
+    }
+    float4* dst = mips[(size_t)chain.n - 1];
+    SE_CUDA(render_mip(chain.level[chain.n - 1], w, h, dst, stream));
+    chain.level[chain.n] = dst;
+    chain.w[chain.n] = nw;
+    chain.h[chain.n] = nh;
+    w = nw;
+    h = nh;
+  }
+  const float4* bgd = nullptr;
+  if (bg) {
+    const size_t bytes = (size_t)bw * bh * sizeof(float4);
+    if (bytes > bg_cap) {
+      if (d_bg) cudaFree(d_bg);
+      d_bg = nullptr;
+      bg_cap = 0;
+      cudaError_t e = cudaMalloc(&d_bg, bytes);
+      if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+      bg_cap = bytes;
+    }
+    SE_CUDA(cudaMemcpyAsync(d_bg, bg, bytes, cudaMemcpyDefault, stream));
+    bgd = d_bg;
+  }
+  if (!d_composite) {
+    cudaError_t e = cudaMalloc(&d_composite, (size_t)W * H * sizeof(float4));
+    if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+  }
+  Timed* t = nullptr;
+  if (timing) {
+    s = timing_begin(3, (long long)W * H, 1, &t);
+    if (!s.ok()) return s;
+  }
+  SE_CUDA(render_composite(chain, light[0] ? light[lcur] : nullptr, bgd, bw, bh, kBlurSideWeight, d_composite,
+                           stream));
   if (t) SE_CUDA(cudaEventRecord(t->b, stream));
   return Status::Ok();
 }

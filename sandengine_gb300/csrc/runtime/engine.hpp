@@ -84,15 +84,16 @@ struct World {
   Status launch_edit(const se_modification* mods, int nlive);
   int default_k() const;
   // Opt-in per-launch CUDA-event timing (for roofline measurements) of the tile kernel
-  // (pass 0), the light pass (1) and the colour pass (2).
+  // (pass 0), the light pass (1), the colour pass (2) and the composite (3, its pyramid
+  // excluded).
   bool timing = false;
   struct Timed {
     cudaEvent_t a, b;
     long long cells;  // cells the launch covered
     int frames;       // frames the launch advanced
   };
-  std::vector<Timed> timed[3];
-  size_t timed_used[3] = {0, 0, 0};
+  std::vector<Timed> timed[4];
+  size_t timed_used[4] = {0, 0, 0, 0};
   Status timing_begin(int pass, long long cells, int frames, Timed** out);
   Status timing_read(int pass, double* ms, long long* launches, long long* cell_frames, long long* cells);
   Status digest(unsigned long long* out);
@@ -110,6 +111,13 @@ struct World {
   Status set_light(bool on);
   Status light_frame();  // light pass for the frame just taken (old grid buf[cur ^ 1])
   Status render_color();  // the current grid's colours into d_color
+  // Headless composite of the current grid (colour, its pyramid, the light field when
+  // kept, an optional background image) into d_composite (RGBA32F per cell).
+  std::vector<float4*> mips;  // colour pyramid levels 1..
+  float4* d_composite = nullptr;
+  float4* d_bg = nullptr;
+  size_t bg_cap = 0;
+  Status composite(const float* bg, int bw, int bh);
 };
 
 // One launch of a single-world tile kernel (se_tile_*): k frames with counters f0.. over

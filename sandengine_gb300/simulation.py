@@ -184,6 +184,25 @@ class Simulation:
         check(lib().se_world_render_color(self._h, out.ctypes.data, out.size))
         return out
 
+    def composite(self, background: Optional[np.ndarray] = None) -> np.ndarray:
+        """Headless composite of the current grid (fragment140.glsl): (H, W, 4) float32 RGBA,
+        rows top to bottom.  ``background``: optional (bh, bw, 4) float32 image."""
+        w, h = self.size
+        out = np.empty((h, w, 4), dtype=np.float32)
+        bg, bw, bh = None, 0, 0
+        if background is not None:
+            bgarr = np.ascontiguousarray(background, dtype=np.float32)
+            assert bgarr.ndim == 3 and bgarr.shape[2] == 4
+            bg, bh, bw = bgarr.ctypes.data, bgarr.shape[0], bgarr.shape[1]
+        check(lib().se_world_composite(self._h, bg, bw, bh, out.ctypes.data, out.size))
+        return out
+
+    def composite_device(self) -> int:
+        """Composite into the world's device buffer (stream-ordered); returns its address."""
+        p = ctypes.c_void_p()
+        check(lib().se_world_composite_device(self._h, None, 0, 0, ctypes.byref(p)))
+        return p.value or 0
+
     def render_color_device(self) -> int:
         """Render output_color into the world's device buffer (stream-ordered); returns its
         address (RGBA32F, height x width x 4)."""

@@ -90,3 +90,28 @@ def test_color_matches_port_within_sin_tolerance(se, rulesets, ports, name):
     assert small >= 0.995 and d.mean() <= 1e-3
     # the same grid again reads the cached noise: identical output
     assert np.array_equal(sim.output_color, got)
+
+
+@pytest.mark.parametrize("shape", [(640, 400), (333, 517), (64, 64)])
+def test_composite_matches_port(se, rulesets, ports, shape):
+    """The headless composite (fragment140.glsl) equals the oracle's restatement bit for bit
+    when both start from the same colour and light fields (the GPU's own), with and
+    without a background image, on non-square and odd-sized worlds."""
+    W, H = shape
+    P = ports["twelve_materials"]
+    rs = se.parse_string(rulesets["twelve_materials"])
+    sim = se.Simulation(rs, (W, H))
+    sim.grid = wl.patch_fill(W, H, 6, *wl.twelve_fill_spec(), patch=16)
+    sim.params.frame = 3
+    sim.set_light(True)
+    sim.run_frames(20)
+    col, light = sim.output_color, sim.output_light
+    bg = np.random.default_rng(2).random((211, 157, 4)).astype(np.float32)
+    got = sim.composite(bg)
+    want = P.composite(col, light, bg)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    got2 = sim.composite()
+    assert np.array_equal(got2.view(np.uint32), P.composite(col, light).view(np.uint32))
+    sim.set_light(False)  # no light field: zero light
+    assert np.array_equal(sim.composite().view(np.uint32), P.composite(col).view(np.uint32))
+    assert np.isfinite(got).all() and got.max() > 0

@@ -171,3 +171,31 @@ def test_port_color_and_light_match_reference_shader(rulesets, name):
             assert np.array_equal(port_light.view(np.uint32), light.view(np.uint32)), f"light, frame {f}"
             g = new
         assert np.count_nonzero(light) > 0
+
+
+def test_port_composite_known_answers(rulesets):
+    """The composite restatement on fields with closed-form answers: an opaque uniform
+    field shades with occlusion 0 (ambient 0.1) and sky light 0.5 * (1 - v'); transparent
+    cells show the background tinted by the same light; the pyramid averages 2x2 blocks."""
+    P = Port(rulesets["four_materials"])
+    H, W = 32, 32
+    color = np.zeros((H, W, 4), dtype=np.float32)
+    color[...] = (0.8, 0.4, 0.2, 1.0)
+    out = P.composite(color)
+    d = np.float32(1.0) / (np.float32(W) / np.float32(2.0))
+    v = (np.arange(H, dtype=np.float32) + np.float32(0.5)) / np.float32(H)
+    pv = np.floor(v / d) * d
+    sky = np.float32(0.5) * (np.float32(1.0) - pv)
+    shade = np.float32(0.1)  # occ = 1 - 1 = 0
+    want_r = np.float32(0.8) * shade * (np.float32(0.1) + sky)
+    assert np.allclose(out[:, 0, 0], want_r, rtol=1e-6, atol=0)
+    assert np.all(out[..., 3] == 1.0)
+    bg = np.random.default_rng(0).random((H, W, 4)).astype(np.float32)
+    clear = np.zeros_like(color)
+    out2 = P.composite(clear, background=bg)
+    # 1:1 bilinear at texel centres of a flipped v: the background's rows reversed
+    assert np.allclose(out2[..., 3], bg[::-1, :, 3], rtol=1e-6, atol=1e-7)
+    lv = P.mips(bg)
+    assert lv[1].shape == (16, 16, 4)
+    assert np.allclose(lv[1], bg.reshape(16, 2, 16, 2, 4).mean(axis=(1, 3)), rtol=1e-6, atol=1e-7)
+    assert lv[-1].shape == (1, 1, 4)
