@@ -212,6 +212,9 @@ __global__ void __launch_bounds__(256) se_light_kernel(const uint32_t* __restric
 
 // ---- headless composite ---------------------------------------------------------------
 __device__ __forceinline__ int mirror_index(int i, int n) {  // GL_MIRRORED_REPEAT on texel indices
+  if ((unsigned)i < (unsigned)n) return i;  // almost every tap
+  if (i == -1) return 0;
+  if (i == n) return n - 1;
   const int p = 2 * n;
   int m = i % p;
   if (m < 0) m += p;
@@ -273,40 +276,72 @@ __global__ void __launch_bounds__(256) se_mip_kernel(const float4* __restrict__ 
                                         fmul(fadd(fadd(fadd(a.w, b.w), c.w), d.w), 0.25f));
 }
 
-__global__ void __launch_bounds__(256) se_composite_kernel(const MipChain m, const float4* __restrict__ light,
-                                                           const float4* __restrict__ bg, int bw, int bh, float ws0,
-                                                           float ws1, float ws2, float4* __restrict__ out) {
-  const int W = m.w[0], H = m.h[0];
-  const int cx = blockIdx.x * 32 + (threadIdx.x & 31), r = blockIdx.y * 8 + (threadIdx.x >> 5);
-  if (cx >= W || r >= H) return;
-  const float pixelate = __fdiv_rn((float)W, 2.0f);
-  const float d = __fdiv_rn(1.0f, pixelate);
-  const float u = __fdiv_rn(fadd((float)cx, 0.5f), (float)W), v = __fdiv_rn(fadd((float)r, 0.5f), (float)H);
-  const float pu = fmul(floorf(__fdiv_rn(u, d)), d), pv = fmul(floorf(__fdiv_rn(v, d)), d);
-  float4 col = sample_nearest(m.level[0], W, H, u, v);  // texture(color_tex, uv, 0.0): 1:1, magnification
-  float4 li = light ? sample_linear(light, W, H, pu, pv) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  li.x = gclamp(li.x, 0.0f, 1.0f);
-  li.y = gclamp(li.y, 0.0f, 1.0f);
-  li.z = gclamp(li.z, 0.0f, 1.0f);
+// The part of a fragment that depends only on the pixelated coordinate (pu, pv): the
+// clamped light and the occlusion.
+struct Shared {
+  float lr, lg, lb, occ;
+};
+__device__ Shared shared_terms(const MipChain& m, const float4* __restrict__ light, float pu, float pv, float ws0,
+                               float ws1, float ws2) {
+  float4 li = light ? sample_linear(light, m.w[0], m.h[0], pu, pv) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   float occ = fsub(1.0f, blurred_alpha(m, pu, pv, 1.0f, ws0));
   const float occ2 = fsub(1.0f, blurred_alpha(m, pu, pv, 4.0f, ws1));
   const float occ3 = fsub(1.0f, blurred_alpha(m, pu, pv, 5.0f, ws2));
   occ = gclamp(fadd(occ, fadd(fmul(occ2, 0.4f), fmul(occ3, 0.25f))), 0.0f, 1.0f);
+  return Shared{gclamp(li.x, 0.0f, 1.0f), gclamp(li.y, 0.0f, 1.0f), gclamp(li.z, 0.0f, 1.0f), occ};
+}
+
+// Thread = 2 x 2 pixels (columns 2k, 2k + 1 share pu; rows share pv when W <= H, else
+// the shared terms are computed per row).
+__global__ void __launch_bounds__(256) se_composite_kernel(const MipChain m, const float4* __restrict__ light,
+                                                           const float4* __restrict__ bg, int bw, int bh, float ws0,
+                                                           float ws1, float ws2, float4* __restrict__ out) {
+  const int W = m.w[0], H = m.h[0];
+  const int c0 = 2 * (blockIdx.x * 32 + (threadIdx.x & 31)), r0 = 2 * (blockIdx.y * 8 + (threadIdx.x >> 5));
+  if (c0 >= W || r0 >= H) return;
+  const float pixelate = __fdiv_rn((float)W, 2.0f);
+  const float d = __fdiv_rn(1.0f, pixelate);
+  const float u0 = __fdiv_rn(fadd((float)c0, 0.5f), (float)W);
+  const float pu = fmul(floorf(__fdiv_rn(u0, d)), d);  // the same for column c0 + 1
+  Shared sh[2];
+  float pvs[2];
+#pragma unroll
+  for (int dr = 0; dr < 2; ++dr) {
+    const int r = r0 + dr;
+    if (r >= H) break;
+    const float v = __fdiv_rn(fadd((float)r, 0.5f), (float)H);
+    pvs[dr] = fmul(floorf(__fdiv_rn(v, d)), d);
+    sh[dr] = (dr == 1 && pvs[1] == pvs[0]) ? sh[0] : shared_terms(m, light, pu, pvs[dr], ws0, ws1, ws2);
+  }
   const float ambient = 0.1f;
-  const float sky = fmul(0.5f, fsub(1.0f, pv));
-  const float shade = fadd(ambient, fmul(occ, fsub(1.0f, ambient)));
-  col.x = gclamp(fmul(col.x, shade), 0.0f, 1.0f);
-  col.y = gclamp(fmul(col.y, shade), 0.0f, 1.0f);
-  col.z = gclamp(fmul(col.z, shade), 0.0f, 1.0f);
-  const float4 b = bg ? sample_linear(bg, bw, bh, u, fsub(1.0f, v)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  const float ia = fsub(1.0f, col.w);
-  const float base = fadd(ambient, sky);
-  float4 o;  // mix(bg, col, col.a) * vec4(ambient + sky + light, 1.0)
-  o.x = fmul(fadd(fmul(b.x, ia), fmul(col.x, col.w)), fadd(base, li.x));
-  o.y = fmul(fadd(fmul(b.y, ia), fmul(col.y, col.w)), fadd(base, li.y));
-  o.z = fmul(fadd(fmul(b.z, ia), fmul(col.z, col.w)), fadd(base, li.z));
-  o.w = fmul(fadd(fmul(b.w, ia), fmul(col.w, col.w)), 1.0f);
-  out[(size_t)r * W + cx] = o;
+#pragma unroll
+  for (int dr = 0; dr < 2; ++dr) {
+    const int r = r0 + dr;
+    if (r >= H) break;
+    const float v = __fdiv_rn(fadd((float)r, 0.5f), (float)H);
+    const Shared& S = sh[dr];
+    const float sky = fmul(0.5f, fsub(1.0f, pvs[dr]));
+    const float shade = fadd(ambient, fmul(S.occ, fsub(1.0f, ambient)));
+    const float base = fadd(ambient, sky);
+#pragma unroll
+    for (int dc = 0; dc < 2; ++dc) {
+      const int cx = c0 + dc;
+      if (cx >= W) break;
+      const float u = __fdiv_rn(fadd((float)cx, 0.5f), (float)W);
+      float4 col = sample_nearest(m.level[0], W, H, u, v);  // texture(color_tex, uv, 0.0): magnification
+      col.x = gclamp(fmul(col.x, shade), 0.0f, 1.0f);
+      col.y = gclamp(fmul(col.y, shade), 0.0f, 1.0f);
+      col.z = gclamp(fmul(col.z, shade), 0.0f, 1.0f);
+      const float4 b = bg ? sample_linear(bg, bw, bh, u, fsub(1.0f, v)) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float ia = fsub(1.0f, col.w);
+      float4 o;  // mix(bg, col, col.a) * vec4(ambient + sky + light, 1.0)
+      o.x = fmul(fadd(fmul(b.x, ia), fmul(col.x, col.w)), fadd(base, S.lr));
+      o.y = fmul(fadd(fmul(b.y, ia), fmul(col.y, col.w)), fadd(base, S.lg));
+      o.z = fmul(fadd(fmul(b.z, ia), fmul(col.z, col.w)), fadd(base, S.lb));
+      o.w = fmul(fadd(fmul(b.w, ia), fmul(col.w, col.w)), 1.0f);
+      out[(size_t)r * W + cx] = o;
+    }
+  }
 }
 
 }  // namespace
@@ -320,7 +355,7 @@ cudaError_t render_mip(const float4* src, int sw, int sh, float4* dst, cudaStrea
 
 cudaError_t render_composite(const MipChain& mips, const float4* light, const float4* bg, int bw, int bh,
                              const float w_side[3], float4* out, cudaStream_t s) {
-  dim3 grid((unsigned)((mips.w[0] + 31) / 32), (unsigned)((mips.h[0] + 7) / 8));
+  dim3 grid((unsigned)((mips.w[0] + 63) / 64), (unsigned)((mips.h[0] + 15) / 16));
   se_composite_kernel<<<grid, 256, 0, s>>>(mips, light, bg, bw, bh, w_side[0], w_side[1], w_side[2], out);
   return cudaGetLastError();
 }
