@@ -305,7 +305,11 @@ def run_ours(args, rep):
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": f"se_tile (k={k})", "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": alg_bytes_per_launch,
-                     "avg_launch_ms": avg_launch_s * 1e3, "kernel_share_of_step": kernel_ms / ms if ms else None},
+                     "avg_launch_ms": avg_launch_s * 1e3, "kernel_share_of_step": kernel_ms / ms if ms else None,
+                     # k frames per launch: 8 B per cell per launch cover k updates.  The
+                     # same updates from one-frame launches would move value * 8 bytes/s.
+                     "unfused_equivalent_gbs": value * 8.0 / 1e9,
+                     "unfused_equivalent_frac": value * 8.0 / 1e9 / peak},
         "gpu_launches": launches + args.steps + sum(p["launches"] for p in passes.values()),
         "clocks": clocks.summary(),
     }
