@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle", "_build")
 
 VARIANTS = [(128, 64, 1), (256, 32, 1), (128, 32, 1), (128, 64, 2), (128, 64, 4), (128, 64, 8),
-            (128, 128, 8), (128, 128, 16), (256, 64, 4), (64, 64, 4)]
+            (128, 128, 8), (128, 128, 16), (256, 64, 4), (64, 64, 4), (256, 128, 8), (192, 128, 8),
+            (256, 128, 4), (256, 64, 8)]
 
 DRIVER = r'''
 alignas(16) uint8_t se_smem[1 << 21];

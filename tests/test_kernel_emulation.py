@@ -26,7 +26,7 @@ def _world(name, w, h, seed):
 
 
 @pytest.mark.parametrize("name", ["reference", "four_materials", "twelve_materials"])
-@pytest.mark.parametrize("shape", [(256, 256), (517, 389), (130, 67), (7, 5)])
+@pytest.mark.parametrize("shape", [(256, 256), (517, 389), (130, 67), (7, 5), (812, 430)])
 def test_tile_variants_match_port(emus, ports, name, shape):
     w, h = shape
     E, P = emus[name], ports[name]
