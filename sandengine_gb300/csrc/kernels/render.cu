@@ -141,7 +141,7 @@ __device__ __forceinline__ float4 light_blend(const float4* sl, const uint8_t* s
                      fadd(fmul(a2, 0.5f), fmul(m2, 0.5f)), a3);
 }
 
-__global__ void __launch_bounds__(256) se_light_kernel(const uint32_t* __restrict__ old_grid,
+__global__ void __launch_bounds__(256, 6) se_light_kernel(const uint32_t* __restrict__ old_grid,
                                                        const uint32_t* __restrict__ new_grid,
                                                        const float4* __restrict__ lin, float4* __restrict__ lout,
                                                        int W, int H, const RenderMat* __restrict__ mats, int nmat) {
@@ -293,7 +293,7 @@ __device__ Shared shared_terms(const MipChain& m, const float4* __restrict__ lig
 
 // Thread = 2 x 2 pixels (columns 2k, 2k + 1 share pu; rows share pv when W <= H, else
 // the shared terms are computed per row).
-__global__ void __launch_bounds__(256) se_composite_kernel(const MipChain m, const float4* __restrict__ light,
+__global__ void __launch_bounds__(256, 5) se_composite_kernel(const MipChain m, const float4* __restrict__ light,
                                                            const float4* __restrict__ bg, int bw, int bh, float ws0,
                                                            float ws1, float ws2, float4* __restrict__ out) {
   const int W = m.w[0], H = m.h[0];
