@@ -42,7 +42,7 @@ UNIT = "cell-updates/s"
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="world16384",
@@ -109,7 +109,7 @@ def load_traffic(cells_per_launch):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples every 200 ms during the timed region."""
+    """nvidia-smi clock / throttle samples every 100 ms during the timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -126,7 +126,7 @@ class ClockSampler:
             os.close(fd)
             self.out = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.out, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -273,14 +273,16 @@ def run_ours(args, rep):
     # (kernel parameters) and the grid comes back into pinned host memory.
     e2e = None
     if not args.no_e2e:
-        host = torch.empty((H, W), dtype=torch.int32, pin_memory=True)
+        # two pinned buffers; each step's grid is snapshotted on the device and copied to the
+        # host on a copy stream while the next step computes
+        hosts = [torch.empty((H, W), dtype=torch.int32, pin_memory=True) for _ in range(2)]
         from sandengine_gb300._lib import check, lib
         rep.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for r in range(args.steps):
             one_step(args.warmup + r)
-            check(lib().se_world_get_grid_async(sim.handle, host.data_ptr(), W * H))
+            check(lib().se_world_read_grid_overlapped(sim.handle, hosts[r & 1].data_ptr(), W * H))
         sim.synchronize()
         e2e_s = rep.max(time.perf_counter() - t0)
         e2e = {"value": rep.sum(updates) / e2e_s, "unit": UNIT,

@@ -176,6 +176,12 @@ int se_world_get_grid(se_world* w, uint32_t* cells, size_t count);
  * stream reaches them. */
 int se_world_set_grid_async(se_world* w, const uint32_t* cells, size_t count);
 int se_world_get_grid_async(se_world* w, uint32_t* cells, size_t count);
+/* Read-back that overlaps the world's next frames: the current grid is copied on the
+ * device into one of two staging buffers (ordered on the world's stream), then to `cells`
+ * (pinned host memory for full overlap; count = width * height) on a separate copy stream.
+ * `cells` holds this grid once se_world_synchronize returns.  At most two such reads are
+ * in flight; a third waits for the first.  (No counterpart in the reference.) */
+int se_world_read_grid_overlapped(se_world* w, uint32_t* cells, size_t count);
 /* Device pointer of the current grid (valid until the next step, which ping-pongs). */
 int se_world_device_grid(se_world* w, uint32_t** device_cells);
 /* Params.frame (simulation.rs:78): the counter before the next step (>= 0). */
@@ -187,6 +193,7 @@ int se_world_get_frame(const se_world* w, int32_t* frame);
  * of these frames only, as the reference clears its list after each run.  Asynchronous on
  * the world's stream. */
 int se_world_step(se_world* w, int nframes, const se_modification* mods, int nmods);
+/* Waits for the world's stream and for its overlapped read-backs. */
 int se_world_synchronize(se_world* w);
 /* Order-independent 64-bit digest of the current grid: sum over cells i of
  * splitmix64_finalize((i << 32) | cell[i]) mod 2^64.  Synchronizes the stream.

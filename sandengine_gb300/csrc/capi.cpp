@@ -370,6 +370,14 @@ SE_API int se_world_get_grid_async(se_world* w, uint32_t* cells, size_t count) {
   return guard([&] { return grid_copy(w, cells, count, false, false); });
 }
 
+SE_API int se_world_read_grid_overlapped(se_world* w, uint32_t* cells, size_t count) {
+  return guard([&] {
+    if (!w || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    if (count != (size_t)w->w->W * w->w->H) return fail(SE_ERR_INVALID_ARGUMENT, "count must be width * height");
+    return ret(w->w->read_grid_overlapped(cells));
+  });
+}
+
 SE_API int se_world_device_grid(se_world* w, uint32_t** p) {
   return guard([&] {
     if (!w || !p) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
@@ -405,9 +413,7 @@ SE_API int se_world_step(se_world* w, int nframes, const se_modification* mods, 
 SE_API int se_world_synchronize(se_world* w) {
   return guard([&] {
     if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
-    cudaError_t e = cudaStreamSynchronize(w->w->stream);
-    if (e != cudaSuccess) return fail(SE_ERR_CUDA, std::string("synchronize: ") + cudaGetErrorString(e));
-    return (int)SE_OK;
+    return ret(w->w->synchronize_all());
   });
 }
 

@@ -89,6 +89,13 @@ World::~World() {
   if (d_noise) cudaFree(d_noise);
   if (d_color) cudaFree(d_color);
   for (auto* m : mips) cudaFree(m);
+  if (copy_stream) cudaStreamSynchronize(copy_stream);
+  for (int i = 0; i < 2; ++i) {
+    if (stage[i]) cudaFree(stage[i]);
+    if (stage_ready[i]) cudaEventDestroy(stage_ready[i]);
+    if (stage_done[i]) cudaEventDestroy(stage_done[i]);
+  }
+  if (copy_stream) cudaStreamDestroy(copy_stream);
   if (d_composite) cudaFree(d_composite);
   if (d_bg) cudaFree(d_bg);
   if (d_scratch) cudaFree(d_scratch);
@@ -472,6 +479,35 @@ Status World::composite(const float* bg, int bw, int bh) {
   SE_CUDA(render_composite(chain, light[0] ? light[lcur] : nullptr, bgd, bw, bh, kBlurSideWeight, d_composite,
                            stream));
   if (t) SE_CUDA(cudaEventRecord(t->b, stream));
+  return Status::Ok();
+}
+
+Status World::read_grid_overlapped(uint32_t* host) {
+  const size_t bytes = (size_t)W * H * sizeof(uint32_t);
+  if (!copy_stream) {
+    SE_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+      cudaError_t e = cudaMalloc(&stage[i], bytes);
+      if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+      SE_CUDA(cudaEventCreateWithFlags(&stage_ready[i], cudaEventDisableTiming));
+      SE_CUDA(cudaEventCreateWithFlags(&stage_done[i], cudaEventDisableTiming));
+      SE_CUDA(cudaEventRecord(stage_done[i], copy_stream));
+    }
+  }
+  const int i = stage_i;
+  stage_i ^= 1;
+  SE_CUDA(cudaStreamWaitEvent(stream, stage_done[i], 0));  // its previous host copy has finished
+  SE_CUDA(cudaMemcpyAsync(stage[i], buf[cur], bytes, cudaMemcpyDeviceToDevice, stream));
+  SE_CUDA(cudaEventRecord(stage_ready[i], stream));
+  SE_CUDA(cudaStreamWaitEvent(copy_stream, stage_ready[i], 0));
+  SE_CUDA(cudaMemcpyAsync(host, stage[i], bytes, cudaMemcpyDeviceToHost, copy_stream));
+  SE_CUDA(cudaEventRecord(stage_done[i], copy_stream));
+  return Status::Ok();
+}
+
+Status World::synchronize_all() {
+  SE_CUDA(cudaStreamSynchronize(stream));
+  if (copy_stream) SE_CUDA(cudaStreamSynchronize(copy_stream));
   return Status::Ok();
 }
 

@@ -118,6 +118,16 @@ struct World {
   float4* d_bg = nullptr;
   size_t bg_cap = 0;
   Status composite(const float* bg, int bw, int bh);
+
+  // Grid read-back overlapped with the next frames: the grid is snapshotted on the world's
+  // stream (device copy into one of two staging buffers) and copied to the host on a copy
+  // stream, so the world's next launches do not wait for the host copy.
+  uint32_t* stage[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t stage_ready[2] = {nullptr, nullptr}, stage_done[2] = {nullptr, nullptr};
+  int stage_i = 0;
+  Status read_grid_overlapped(uint32_t* host);
+  Status synchronize_all();  // the world's stream and the copy stream
 };
 
 // One launch of a single-world tile kernel (se_tile_*): k frames with counters f0.. over

@@ -123,6 +123,13 @@ class Simulation:
             raise ValueError(f"grid must have shape {(h, w)}, got {a.shape}")
         check(lib().se_world_set_grid(self._h, a.ctypes.data, a.size))
 
+    def read_grid_overlapped(self, out: np.ndarray) -> None:
+        """Start copying the current grid into ``out`` ((H, W) uint32, ideally pinned) without
+        holding back the next frames; ``out`` is filled once synchronize() returns."""
+        w, h = self.size
+        assert out.shape == (h, w) and out.dtype == np.uint32 and out.flags.c_contiguous
+        check(lib().se_world_read_grid_overlapped(self._h, out.ctypes.data, out.size))
+
     def device_grid_ptr(self) -> int:
         p = ctypes.c_void_p()
         check(lib().se_world_device_grid(self._h, ctypes.byref(p)))

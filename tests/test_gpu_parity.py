@@ -175,3 +175,28 @@ def test_device_table_matches_emulated_rules(se, rulesets, name):
     assert np.array_equal(table, want_t)
     assert np.array_equal(bits, want_b)
     assert 0 < int(np.unpackbits(bits.view(np.uint8)).sum()) < 32 * bits.size
+
+
+def test_overlapped_read_back_returns_each_steps_grid(se, rulesets, ports):
+    """se_world_read_grid_overlapped: two read-backs in flight, then a third that waits for
+    the first; after synchronize each buffer holds the grid of the step it was issued after."""
+    from sandengine_gb300 import workloads as wl
+    P = ports["twelve_materials"]
+    rs = se.parse_string(rulesets["twelve_materials"])
+    W, H = 300, 220
+    g = wl.patch_fill(W, H, 8, *wl.twelve_fill_spec(), patch=16)
+    sim = se.Simulation(rs, (W, H))
+    sim.grid = g
+    sim.params.frame = 2
+    outs, wants, f = [], [], 2
+    for r in range(3):
+        sim.run_frames(7)
+        P.run(g, f, 7)
+        f += 7
+        o = np.empty((H, W), dtype=np.uint32)
+        sim.read_grid_overlapped(o)
+        outs.append(o)
+        wants.append(g.copy())
+    sim.synchronize()
+    for o, w in zip(outs, wants):
+        assert np.array_equal(o, w)
