@@ -317,6 +317,27 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int gx0, 
   }
 }
 
+// Updates the chunk (4 blocks, 8 x 2 cells) at p, row stride SW, whose first block's hash
+// base is x, with word-wide shared-memory access.
+template <int OX>
+__device__ __forceinline__ void se_chunk_eval(uint8_t* p, int SW, uint32_t x, const uint16_t* __restrict__ lut) {
+  uint32_t a0, a1, b0, b1;
+  se_ld8<OX>(p, a0, a1);
+  se_ld8<OX>(p + SW, b0, b1);
+  // [a, b, c, d] of the four blocks; block origins are 2 cells apart (x + 922 each).  No
+  // branch on all-EMPTY blocks (the table maps them to themselves), so the four lookups are
+  // in flight together.
+  const uint32_t i0 = se_lut_word_index(__byte_perm(a0, b0, 0x5410), x);
+  const uint32_t i1 = se_lut_word_index(__byte_perm(a0, b0, 0x7632), x + 922u);
+  const uint32_t i2 = se_lut_word_index(__byte_perm(a1, b1, 0x5410), x + 1844u);
+  const uint32_t i3 = se_lut_word_index(__byte_perm(a1, b1, 0x7632), x + 2766u);
+  const uint32_t o0 = se_lut_fetch(lut, i0), o1 = se_lut_fetch(lut, i1), o2 = se_lut_fetch(lut, i2),
+                 o3 = se_lut_fetch(lut, i3);
+  const uint32_t B0 = se_lut_bytes(o0), B1 = se_lut_bytes(o1), B2 = se_lut_bytes(o2), B3 = se_lut_bytes(o3);
+  se_st8<OX>(p, __byte_perm(B0, B1, 0x5410), __byte_perm(B2, B3, 0x5410));
+  se_st8<OX>(p + SW, __byte_perm(B0, B1, 0x7632), __byte_perm(B2, B3, 0x7632));
+}
+
 template <int SW, int OX, int NT>
 __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int gx0,
                                                  int gy0, int f, const uint16_t* __restrict__ lut) {
@@ -324,23 +345,8 @@ __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __
   for (int i = threadIdx.x; i < n; i += NT) {
     const int off = list[i];
     const int ly = off / SW, lx = off - ly * SW;
-    uint8_t* p = sm + off;
-    uint32_t a0, a1, b0, b1;
-    se_ld8<OX>(p, a0, a1);
-    se_ld8<OX>(p + SW, b0, b1);
     const uint32_t x = (uint32_t)(gx0 + lx) * 461u + (uint32_t)(gy0 + ly) * 2131u + xf;
-    // [a, b, c, d] of the four blocks; block origins are 2 cells apart (x + 922 each).  No
-    // branch on all-EMPTY blocks (the table maps them to themselves), so the four lookups
-    // are in flight together.
-    const uint32_t i0 = se_lut_word_index(__byte_perm(a0, b0, 0x5410), x);
-    const uint32_t i1 = se_lut_word_index(__byte_perm(a0, b0, 0x7632), x + 922u);
-    const uint32_t i2 = se_lut_word_index(__byte_perm(a1, b1, 0x5410), x + 1844u);
-    const uint32_t i3 = se_lut_word_index(__byte_perm(a1, b1, 0x7632), x + 2766u);
-    const uint32_t o0 = se_lut_fetch(lut, i0), o1 = se_lut_fetch(lut, i1), o2 = se_lut_fetch(lut, i2),
-                   o3 = se_lut_fetch(lut, i3);
-    const uint32_t B0 = se_lut_bytes(o0), B1 = se_lut_bytes(o1), B2 = se_lut_bytes(o2), B3 = se_lut_bytes(o3);
-    se_st8<OX>(p, __byte_perm(B0, B1, 0x5410), __byte_perm(B2, B3, 0x5410));
-    se_st8<OX>(p + SW, __byte_perm(B0, B1, 0x7632), __byte_perm(B2, B3, 0x7632));
+    se_chunk_eval<OX>(sm + off, SW, x, lut);
   }
 }
 #endif

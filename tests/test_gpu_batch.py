@@ -67,3 +67,43 @@ def test_batch_autotune_keeps_state(se, rulesets):
     assert k >= 1
     for i, g in enumerate(gs):
         assert np.array_equal(b.grid(i), g) and b.frame(i) == 2
+
+
+def test_rules_that_set_wall_cells_keep_the_world_border(se, rulesets):
+    """A rule that SETs a WALL neighbour (WALL's density singles it out) on worlds with WALL
+    cells inside: single-world launches (k = 1 and 8) and a batch with resident and tiled
+    worlds equal the oracle; the WALL outside the world is never written."""
+    from oracle.build import Port
+    from sandengine_gb300 import workloads as wl
+    from sandengine_gb300.batch import Batch
+    from tests.test_kernel_emulation import WALL_RULE
+    text = rulesets["four_materials"].replace("rules:\n", "rules:\n" + WALL_RULE.lstrip("\n"), 1)
+    text = text.replace("base_rules: [fall]", "base_rules: [fall, paint_wall]")
+    rs, P = se.parse_string(text), Port(text)
+    rng = np.random.default_rng(5)
+    sizes = [(137, 61), (300, 150), (1100, 700), (33, 17)]
+    grids = []
+    for W, H in sizes:
+        g = wl.iid_fill(W, H, 4, *wl.FOUR_FILL)
+        g[rng.random((H, W)) < 0.05] = 2
+        grids.append(g)
+    for (W, H), g in zip(sizes, grids):
+        for k in (1, 8):
+            sim = se.Simulation(rs, (W, H))
+            sim.set_steps_per_launch(k)
+            sim.grid = g
+            sim.params.frame = 4
+            sim.run_frames(24)
+            want = g.copy()
+            P.run(want, 4, 24)
+            assert np.array_equal(sim.grid, want), f"{W}x{H} k={k}"
+    b = Batch(rs, sizes)
+    for i, g in enumerate(grids):
+        b.set_grid(i, g)
+        b.set_frame(i, 4)
+    b.step(30)
+    b.synchronize()
+    for i, g in enumerate(grids):
+        want = g.copy()
+        P.run(want, 4, 30)
+        assert np.array_equal(b.grid(i), want), f"batch world {i} {sizes[i]}"

@@ -143,3 +143,42 @@ def test_band_window_matches_port(emus, ports, name):
         lo = 0 if ya == 0 else n
         hi = (yb - ya) if yb == H else (yb - ya) - n
         assert np.array_equal(buf[lo:hi], want[ya + lo:ya + hi]), f"band [{ya}, {yb}) launches {launches}"
+
+
+WALL_RULE = """
+  paint_wall:
+    if: RIGHT.mat.density > 5000.0
+    do: SET RIGHT sand
+    else:
+      if: DOWN.mat.density > 5000.0
+      do: SET DOWN water
+"""
+
+
+def test_rules_that_set_wall_cells_keep_the_world_border(se, rulesets, ports):
+    """A rule that SETs a WALL neighbour (rule text cannot name WALL, but WALL's density of
+    9999 singles it out) changes WALL cells inside the world but never the WALL outside it
+    (getCell returns WALL there and no invocation writes it): the tile, whole-world and
+    serving kernels on worlds whose edges and interior hold WALL cells."""
+    from oracle.build import Port
+    text = rulesets["four_materials"].replace("rules:\n", "rules:\n" + WALL_RULE.lstrip("\n"), 1)
+    text = text.replace("base_rules: [fall]", "base_rules: [fall, paint_wall]")
+    rs = se.parse_string(text)
+    assert "SE_LUT 1" in rs.cuda_source
+    E, P = Emu(rs, lut=True), Port(text)
+    rng = np.random.default_rng(12)
+    for W, H in ((137, 61), (40, 33), (300, 150)):
+        g = wl.iid_fill(W, H, 4, *wl.FOUR_FILL)
+        g[rng.random((H, W)) < 0.05] = 2  # WALL inside the world
+        for v in ((128, 64, 1), (128, 64, 8), (64, 64, 4), (256, 128, 8)):
+            want = g.copy()
+            P.run(want, 4, v[2])
+            assert np.array_equal(E.tiles(g, 5, v[2], v), want), f"tile {v} {W}x{H}"
+        out, _ = E.batch([g], [4], 9, 4, [0])  # whole world resident in shared memory
+        want = g.copy()
+        P.run(want, 4, 9)
+        assert np.array_equal(out[0], want), f"resident {W}x{H}"
+        got = E.serve_iteration([g], [4], [8])[0]
+        want = g.copy()
+        P.run(want, 4, 8)
+        assert np.array_equal(got, want), f"serving {W}x{H}"
