@@ -48,6 +48,8 @@ def parse_args():
     ap.add_argument("--workload", default="world16384",
                     choices=["world16384", "world8192", "world4096", "world256", "batch4096", "serve"])
     ap.add_argument("--worlds", type=int, default=4096, help="batch4096: number of worlds")
+    ap.add_argument("--resident-limit", type=int, default=None,
+                    help="batch4096: shared-memory bytes up to which a world stays resident (0: none)")
     ap.add_argument("--k", type=int, default=0, help="frames per launch (0 = autotuned)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -353,6 +355,8 @@ def run_batch(args, rep):
     sizes = wl.batch_sizes(args.worlds, 4)
     rs = se.parse_string(wl.ruleset_text("twelve_materials"))
     b = Batch(rs, sizes)
+    if args.resident_limit is not None:
+        b.set_resident_limit(args.resident_limit)
     spec = wl.twelve_fill_spec()
     for i, (w, h) in enumerate(sizes):
         b.set_grid(i, wl.patch_fill(w, h, 1000 + i, *spec, patch=16))

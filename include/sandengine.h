@@ -260,6 +260,10 @@ int se_batch_step_plain(se_batch* b, int nframes);
  * the fastest; *best_k = frames per tile pass. */
 int se_batch_autotune(se_batch* b, int reps, int* best_k);
 int se_batch_set_steps_per_launch(se_batch* b, int k);
+/* Worlds whose whole-world CTA needs at most `bytes` of shared memory are advanced in
+ * shared memory for all frames of a launch group; the others by tile passes (0: all by tile
+ * passes).  The default is the device's opt-in maximum. */
+int se_batch_set_resident_limit(se_batch* b, size_t bytes);
 int se_batch_synchronize(se_batch* b);
 int se_batch_get_stream(se_batch* b, void** cuda_stream);
 int se_batch_info(const se_batch* b, int* resident_worlds, int* tiled_worlds, long long* cells,

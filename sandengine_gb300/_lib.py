@@ -102,6 +102,7 @@ _SIGS = {
     "se_batch_step_plain": ([_P, _I], _I),
     "se_batch_autotune": ([_P, _I, ctypes.POINTER(_I)], _I),
     "se_batch_set_steps_per_launch": ([_P, _I], _I),
+    "se_batch_set_resident_limit": ([_P, ctypes.c_size_t], _I),
     "se_batch_synchronize": ([_P], _I),
     "se_batch_get_stream": ([_P, ctypes.POINTER(_P)], _I),
     "se_batch_info": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_longlong),

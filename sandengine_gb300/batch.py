@@ -70,6 +70,10 @@ class Batch:
     def set_steps_per_launch(self, k: int) -> None:
         check(lib().se_batch_set_steps_per_launch(self._h, int(k)))
 
+    def set_resident_limit(self, nbytes: int) -> None:
+        """Keep worlds needing at most ``nbytes`` of shared memory resident (0: none)."""
+        check(lib().se_batch_set_resident_limit(self._h, int(nbytes)))
+
     def synchronize(self) -> None:
         check(lib().se_batch_synchronize(self._h))
 

@@ -576,6 +576,13 @@ SE_API int se_batch_set_steps_per_launch(se_batch* b, int k) {
   });
 }
 
+SE_API int se_batch_set_resident_limit(se_batch* b, size_t bytes) {
+  return guard([&] {
+    if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");
+    return ret(b->b->set_resident_limit(bytes));
+  });
+}
+
 SE_API int se_batch_synchronize(se_batch* b) {
   return guard([&] {
     if (!b) return fail(SE_ERR_INVALID_ARGUMENT, "null batch");

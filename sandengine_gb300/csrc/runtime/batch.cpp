@@ -68,23 +68,39 @@ Status Batch::create(std::shared_ptr<Ruleset> r, int count, const int* widths, c
   SE_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   SE_CUDA(cudaMemsetAsync(arena, 0, bytes, stream));
   desc.resize((size_t)n);
+  for (int i = 0; i < n; ++i)
+    desc[(size_t)i] = WorldDesc{reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(arena) + off[2 * (size_t)i]),
+                                reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(arena) + off[2 * (size_t)i + 1]),
+                                widths[i], heights[i], 0, 0, 0, 0};
+  resident_limit = rs->module->max_dyn_smem;
+  s = classify();
+  if (!s.ok()) return s;
+  SE_CUDA(cudaMalloc(&d_desc, sizeof(WorldDesc) * (size_t)n));
+  s = upload_desc();
+  if (!s.ok()) return s;
+  SE_CUDA(cudaStreamSynchronize(stream));
+  return Status::Ok();
+}
+
+Status Batch::classify() {
   const size_t maxsm = rs->module->max_dyn_smem;
   const LutShape lut = rs->lut_shape();
   // size classes for whole-world CTAs: occupancy is set by the largest world of a class
   const size_t class_max[3] = {40 * 1024, 100 * 1024, maxsm};
   const int class_threads[3] = {256, 512, 1024};
+  for (auto& R : resident)
+    if (R.d_ids) cudaFree(R.d_ids);
   resident.assign(3, Resident{});
+  tiled.clear();
   for (int i = 0; i < n; ++i) {
-    desc[(size_t)i] = WorldDesc{reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(arena) + off[2 * (size_t)i]),
-                                reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(arena) + off[2 * (size_t)i + 1]),
-                                widths[i], heights[i], 0, 0, 0, 0};
-    const size_t rb = resident_bytes(widths[i], heights[i], lut);
+    const size_t rb = resident_bytes(desc[(size_t)i].W, desc[(size_t)i].H, lut);
     int cls = -1;
-    for (int c = 0; c < 3; ++c)
-      if (rb <= class_max[c]) {
-        cls = c;
-        break;
-      }
+    if (rb <= resident_limit)
+      for (int c = 0; c < 3; ++c)
+        if (rb <= class_max[c]) {
+          cls = c;
+          break;
+        }
     if (cls < 0) tiled.push_back(i);
     else resident[(size_t)cls].ids.push_back(i);
   }
@@ -100,11 +116,16 @@ Status Batch::create(std::shared_ptr<Ruleset> r, int count, const int* widths, c
       SE_CUDA(cudaMemcpyAsync(R.d_ids, R.ids.data(), R.ids.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
     }
   }
-  SE_CUDA(cudaMalloc(&d_desc, sizeof(WorldDesc) * (size_t)n));
-  s = upload_desc();
-  if (!s.ok()) return s;
   SE_CUDA(cudaStreamSynchronize(stream));
   return Status::Ok();
+}
+
+Status Batch::set_resident_limit(size_t bytes) {
+  resident_limit = bytes;
+  Status s = classify();
+  if (!s.ok()) return s;
+  if (variant) return set_variant(variant);  // the tile job list
+  return invalidate_graphs();
 }
 
 Status Batch::upload_desc() {

@@ -60,8 +60,13 @@ struct Batch {
   Status autotune(int reps, int* best_k);
   Status set_variant(const TileVariant* v);
   Status invalidate_graphs();
+  // Worlds whose whole-world CTA needs at most `bytes` of shared memory stay resident; the
+  // others take tile passes (0: none resident).  Rebuilds the classes and the job list.
+  Status set_resident_limit(size_t bytes);
+  size_t resident_limit = 0;
 
  private:
+  Status classify();
   Status launch_body(int nframes, cudaStream_t s);
   Status upload_desc();
 };
