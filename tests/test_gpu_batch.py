@@ -107,3 +107,30 @@ def test_rules_that_set_wall_cells_keep_the_world_border(se, rulesets):
         want = g.copy()
         P.run(want, 4, 30)
         assert np.array_equal(b.grid(i), want), f"batch world {i} {sizes[i]}"
+
+
+def test_resident_limit_reclassifies_and_stays_exact(se, ports, rulesets):
+    """se_batch_set_resident_limit moves worlds between whole-world CTAs and tile passes
+    between steps; every world stays equal to the oracle."""
+    from sandengine_gb300 import workloads as wl
+    from sandengine_gb300.batch import Batch
+    sizes = [(96, 64), (300, 200), (33, 17), (700, 500)]
+    rs = se.parse_string(rulesets["twelve_materials"])
+    b = Batch(rs, sizes)
+    grids = [wl.patch_fill(w, h, 40 + i, *wl.twelve_fill_spec(), patch=16) for i, (w, h) in enumerate(sizes)]
+    for i, g in enumerate(grids):
+        b.set_grid(i, g)
+        b.set_frame(i, 2)
+    frames = [2] * len(sizes)
+    port = ports["twelve_materials"]
+    resident_counts = []
+    for limit, nf in ((0, 20), (1 << 30, 17), (20000, 25)):
+        b.set_resident_limit(limit)
+        resident_counts.append(b.info()["resident_worlds"])
+        b.step(nf)
+        b.synchronize()
+        for i, g in enumerate(grids):
+            port.run(g, frames[i], nf, nthreads=8)
+            frames[i] += nf
+            assert np.array_equal(b.grid(i), g), f"limit {limit}, world {i}"
+    assert resident_counts[0] == 0 and resident_counts[1] >= 3 and 0 < resident_counts[2] < resident_counts[1]
