@@ -488,24 +488,51 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   const int gx0 = X0 - HX, gy0 = Y0 - HY;
   const bool vec = (W & 3) == 0;
 
-  for (int i = threadIdx.x; i < WPR * SH; i += NT) {
-    const int r = i / WPR, c = i - r * WPR;
-    const int gy = gy0 + r, gx = gx0 + 4 * c;
-    uint32_t packed;
-    if (gy < ya || gy >= yb) {
-      packed = 0x02020202u;
-    } else if (vec && gx >= 0 && gx + 3 < W) {
-      const uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (size_t)(gy - ya) * W + gx));
-      packed = se_norm(v.x) | (se_norm(v.y) << 8) | (se_norm(v.z) << 16) | (se_norm(v.w) << 24);
-    } else {
-      packed = 0;
-      for (int e = 0; e < 4; ++e) {
-        const int x = gx + e;
-        const uint32_t id = (x >= 0 && x < W) ? se_norm(__ldg(src + (size_t)(gy - ya) * W + x)) : SE_WALL;
-        packed |= id << (8 * e);
+  if (vec && gx0 >= 0 && gy0 >= ya && gx0 + SW <= W && gy0 + SH <= yb) {
+    // The region lies inside the world (and the buffer): four 16-byte loads per thread are
+    // issued before any is converted, so they are in flight together.
+    constexpr int NL = WPR * SH;
+    const uint32_t* base = src + (size_t)(gy0 - ya) * W + gx0;
+    for (int i0 = threadIdx.x; i0 < NL; i0 += 4 * NT) {
+      uint4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + u * NT;
+        if (i < NL) {
+          const int r = i / WPR, c = i - r * WPR;
+          v[u] = __ldg(reinterpret_cast<const uint4*>(base + (size_t)r * W + 4 * c));
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + u * NT;
+        if (i < NL) {
+          const int r = i / WPR, c = i - r * WPR;
+          *reinterpret_cast<uint32_t*>(sm + r * SW + 4 * c) =
+              se_norm(v[u].x) | (se_norm(v[u].y) << 8) | (se_norm(v[u].z) << 16) | (se_norm(v[u].w) << 24);
+        }
       }
     }
-    *reinterpret_cast<uint32_t*>(sm + r * SW + 4 * c) = packed;
+  } else {
+    for (int i = threadIdx.x; i < WPR * SH; i += NT) {
+      const int r = i / WPR, c = i - r * WPR;
+      const int gy = gy0 + r, gx = gx0 + 4 * c;
+      uint32_t packed;
+      if (gy < ya || gy >= yb) {
+        packed = 0x02020202u;
+      } else if (vec && gx >= 0 && gx + 3 < W) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(src + (size_t)(gy - ya) * W + gx));
+        packed = se_norm(v.x) | (se_norm(v.y) << 8) | (se_norm(v.z) << 16) | (se_norm(v.w) << 24);
+      } else {
+        packed = 0;
+        for (int e = 0; e < 4; ++e) {
+          const int x = gx + e;
+          const uint32_t id = (x >= 0 && x < W) ? se_norm(__ldg(src + (size_t)(gy - ya) * W + x)) : SE_WALL;
+          packed |= id << (8 * e);
+        }
+      }
+      *reinterpret_cast<uint32_t*>(sm + r * SW + 4 * c) = packed;
+    }
   }
   __syncthreads();
 
