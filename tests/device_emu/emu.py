@@ -23,6 +23,13 @@ DRIVER = r'''
 alignas(16) uint8_t se_smem[1 << 21];
 static uint16_t* g_lut = nullptr;
 extern "C" const uint16_t* emu_lut() { return g_lut; }
+extern "C" uint32_t emu_lut_index_key(uint32_t i, uint32_t h0, uint32_t h1, uint32_t h2, uint32_t h3) {
+#ifdef SE_LUT
+  return se_gen::lut_index_key(i, h0, h1, h2, h3);
+#else
+  return 0;
+#endif
+}
 extern "C" const uint32_t* emu_static() {
 #ifdef SE_LUT
   return reinterpret_cast<const uint32_t*>(reinterpret_cast<const uint8_t*>(g_lut) + SE_LUT_STATIC_OFF);

@@ -182,3 +182,39 @@ def test_rules_that_set_wall_cells_keep_the_world_border(se, rulesets, ports):
         want = g.copy()
         P.run(want, 4, 8)
         assert np.array_equal(got, want), f"serving {W}x{H}"
+
+
+@pytest.mark.parametrize("name", ["four_materials", "twelve_materials"])
+def test_lut_index_classes_at_every_boundary(se, rulesets, name):
+    """lut_index_key's class per hash lane equals #{thresholds <= h} at every threshold and
+    its neighbours, every multiple of 2^24 and its predecessor, 0 and 2^32 - 1."""
+    import ctypes
+    import re
+    rs = se.parse_string(rulesets[name])
+    src = rs.kernel_source
+    dec = src[src.index("lut_decode("):]
+    dec = dec[:dec.index("\n}\n")]
+    lanes = {}
+    for m in re.finditer(r"const uint32_t reps\[(\d+)\] = \{([^}]*)\}; h(\d) = ", dec):
+        lanes[int(m.group(3))] = [int(v.rstrip("u")) for v in m.group(2).split(",")][1:]
+    assert lanes
+    E = Emu(rs, lut=True)
+    f = E.lib.emu_lut_index_key
+    f.restype = ctypes.c_uint32
+    f.argtypes = [ctypes.c_uint32] * 5
+    for lane, T in lanes.items():
+        probes = {0, 0xFFFFFFFF}
+        for t in T:
+            probes |= {max(0, t - 1), t, min(0xFFFFFFFF, t + 1)}
+        for b in range(256):
+            probes |= {b << 24, max(0, (b << 24) - 1)}
+        others = {l: 0 for l in lanes}  # class 0 in the other lanes
+        for h in sorted(probes):
+            hs = [others.get(l, 0) for l in range(4)]
+            hs[lane] = h
+            got = f(0, *hs)
+            # index = sum over lanes of class * (product of later lanes' class counts)
+            want = 0
+            for l in sorted(lanes):
+                want = want * (len(lanes[l]) + 1) + (sum(1 for t in lanes[l] if t <= hs[l]) if l == lane else 0)
+            assert got == want, f"lane {lane} h={h:#x}: {got} != {want}"
