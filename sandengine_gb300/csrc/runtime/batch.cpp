@@ -1,4 +1,5 @@
 #include "batch.hpp"
+#include "trace.hpp"
 
 #include <algorithm>
 #include <climits>
@@ -269,6 +270,7 @@ Status Batch::autotune(int reps, int* best_k) {
 }
 
 Status Batch::step(int F) {
+  TraceRange trace("se_batch_step");
   if (F < 0) return {SE_ERR_INVALID_ARGUMENT, "nframes must be >= 0"};
   if (F == 0) return Status::Ok();
   int zero = 0;

@@ -1,4 +1,5 @@
 #include "engine.hpp"
+#include "trace.hpp"
 
 #include <algorithm>
 #include <cstring>
@@ -150,6 +151,7 @@ static const TileVariant* pick_variant(int k) {
 }
 
 Status World::autotune(int reps, int* best_k) {
+  TraceRange trace("se_world_autotune");
   if (reps < 1) reps = 1;
   const int f0 = frame + 1 >= 2 ? frame + 1 : 2;  // trial frames never hit the frame-1 clear
   struct Restore {
@@ -308,6 +310,7 @@ Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int row0, int ro
 }
 
 Status World::step(int nframes, const se_modification* mods, int nmods) {
+  TraceRange trace("se_world_step");
   if (nframes < 0) return {SE_ERR_INVALID_ARGUMENT, "nframes must be >= 0"};
   if (nmods < 0 || (nmods > 0 && !mods)) return {SE_ERR_INVALID_ARGUMENT, "bad modification list"};
   if ((int64_t)frame + nframes > INT32_MAX) return {SE_ERR_INVALID_ARGUMENT, "frame counter would overflow i32"};
@@ -408,6 +411,7 @@ Status World::light_frame() {
 }
 
 Status World::render_color() {
+  TraceRange trace("se_world_render_color");
   if (halo >= 0) return {SE_ERR_INVALID_ARGUMENT, "colours are rendered for whole worlds"};
   if (!d_noise) {
     cudaError_t e = cudaMalloc(&d_noise, (size_t)W * H * sizeof(float));
@@ -429,6 +433,7 @@ Status World::render_color() {
 }
 
 Status World::composite(const float* bg, int bw, int bh) {
+  TraceRange trace("se_world_composite");
   if (bg && (bw <= 0 || bh <= 0)) return {SE_ERR_INVALID_ARGUMENT, "background size must be positive"};
   Status s = render_color();
   if (!s.ok()) return s;

@@ -1,4 +1,5 @@
 #include "server.hpp"
+#include "trace.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -237,6 +238,7 @@ Status Server::run(bool plain) {
 // plans iterations ahead of the GPU (at most two in flight) and timestamps completions with
 // events.
 Status Server::run_batched() {
+  TraceRange trace("se_server_run_batched");
   std::vector<int> pend;
   for (size_t i = first_pending; i < requests.size(); ++i) pend.push_back((int)i);
   std::stable_sort(pend.begin(), pend.end(),
@@ -382,6 +384,7 @@ Status Server::run_batched() {
 // One request at a time in arrival order, one launch per frame (plus the edit pass after
 // its first frame): the way the reference advances a world.
 Status Server::run_plain() {
+  TraceRange trace("se_server_run_plain");
   std::vector<int> pend;
   for (size_t i = first_pending; i < requests.size(); ++i) pend.push_back((int)i);
   std::stable_sort(pend.begin(), pend.end(),
