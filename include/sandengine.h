@@ -87,6 +87,15 @@ int se_ruleset_text(const se_ruleset* rs, int which, char* buf, size_t cap, size
 /* Compiles the rule set's kernels for sm_103a with NVRTC (cached on disk under
  * $SE_CACHE_DIR or ~/.cache/sandengine_gb300).  Needs no GPU. */
 int se_ruleset_compile(se_ruleset* rs);
+/* CHECKED build (no counterpart in the reference; the sanitizer substitute): before the
+ * rule set is first compiled, enable != 0 compiles its kernels with index checks on every
+ * shared-memory, global and table access that could leave its buffer.  A failed check sets
+ * a bit of the module's check word and skips the access (no trap).  Bits: 1 table index,
+ * 2 shared-array index, 4 chunk-list capacity, 8 chunk window, 16 global index, 32 edit
+ * index.  se_ruleset_check_word synchronizes the device and reads (and with reset != 0
+ * clears) the word; it covers every world, batch and server of the rule set. */
+int se_ruleset_set_checked(se_ruleset* rs, int enable);
+int se_ruleset_check_word(se_ruleset* rs, unsigned int* word, int reset);
 /* Number of materials (ids 0..n-1; EMPTY=0, NULL=1, WALL=2, then YAML order). */
 int se_ruleset_num_materials(const se_ruleset* rs, int* n);
 /* Material id by name (materials.rs ids), or SE_ERR_NOT_FOUND. */

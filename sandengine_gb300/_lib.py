@@ -70,6 +70,8 @@ _SIGS = {
     "se_world_create_band": ([_P, _I, _I, _I, _I, _I, ctypes.POINTER(_P)], _I),
     "se_world_band_info": ([_P] + [ctypes.POINTER(_I)] * 4, _I),
     "se_world_copy_rows": ([_P, _I, _I, _P, _I], _I),
+    "se_ruleset_set_checked": ([_P, _I], _I),
+    "se_ruleset_check_word": ([_P, ctypes.POINTER(ctypes.c_uint), _I], _I),
     "se_ruleset_table": ([_P, _P, ctypes.c_size_t, _P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_ulonglong),
                           ctypes.POINTER(ctypes.c_ulonglong)], _I),
     "se_ruleset_free": ([_P], None),

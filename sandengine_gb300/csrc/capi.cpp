@@ -108,7 +108,7 @@ SE_API int se_ruleset_text(const se_ruleset* rs, int which, char* buf, size_t ca
     if (which == 0) s = &rs->rs->materials_glsl;
     else if (which == 1) s = &rs->rs->rules_glsl;
     else if (which == 2) s = &rs->rs->cuda.source;
-    else if (which == 3) s = &(full = se::rt::kernel_source(rs->rs->cuda.source));
+    else if (which == 3) s = &(full = rs->rs->device_source());
     else return fail(SE_ERR_INVALID_ARGUMENT, "which must be 0, 1, 2 or 3");
     if (len) *len = s->size();
     if (buf && cap) {
@@ -118,6 +118,23 @@ SE_API int se_ruleset_text(const se_ruleset* rs, int which, char* buf, size_t ca
       if (n < s->size()) return fail(SE_ERR_BUFFER_TOO_SMALL, "buffer too small");
     }
     return (int)SE_OK;
+  });
+}
+
+SE_API int se_ruleset_set_checked(se_ruleset* rs, int enable) {
+  return guard([&] {
+    if (!rs) return fail(SE_ERR_INVALID_ARGUMENT, "null ruleset");
+    std::lock_guard<std::mutex> g(rs->rs->mu);
+    if (rs->rs->compiled) return fail(SE_ERR_INVALID_ARGUMENT, "the rule set is already compiled");
+    rs->rs->checked = enable != 0;
+    return (int)SE_OK;
+  });
+}
+
+SE_API int se_ruleset_check_word(se_ruleset* rs, unsigned int* word, int reset) {
+  return guard([&] {
+    if (!rs || !word) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(rs->rs->check_word(word, reset != 0));
   });
 }
 

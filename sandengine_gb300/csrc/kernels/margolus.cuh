@@ -114,6 +114,21 @@ extern "C" __global__ void __launch_bounds__(256) se_build_static(uint16_t* __re
 }
 #endif
 
+// Index checks of the CHECKED build (module compiled with SE_CHECKED): a failed check sets
+// its bit in se_check_word and the access is skipped (or the index clamped) instead of
+// trapping, so the host can read what went wrong and the context stays usable.  Bits: 1
+// table index, 2 shared-array index, 4 chunk-list capacity, 8 chunk window, 16 global
+// index, 32 edit index.  Without SE_CHECKED every check is the constant true.
+#ifdef SE_CHECKED
+__device__ unsigned int se_check_word;
+__device__ __forceinline__ bool se_check(bool ok, unsigned int bit) {
+  if (!ok) atomicOr(&se_check_word, bit);
+  return ok;
+}
+#else
+__device__ __forceinline__ constexpr bool se_check(bool, unsigned int) { return true; }
+#endif
+
 // One block's update: the block transition table when the rule set has one, else the
 // generated rules.
 __device__ __forceinline__ void se_block_update(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d, int gx, int gy,
@@ -121,7 +136,8 @@ __device__ __forceinline__ void se_block_update(uint32_t& a, uint32_t& b, uint32
 #ifdef SE_LUT
   const uint32_t x = (uint32_t)gx * 461u + (uint32_t)gy * 2131u + (uint32_t)f * 4541161u;
   const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u), h3 = se_mix(x * 213132u);
-  const uint32_t idx = se_gen::lut_index(a, b, c, d, h0, h1, h2, h3);
+  uint32_t idx = se_gen::lut_index(a, b, c, d, h0, h1, h2, h3);
+  if (!se_check(idx < SE_LUT_ENTRIES, 1u)) idx = 0;
 #if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
   const uint32_t o = lut[idx];  // shared-memory copy
 #else
@@ -166,6 +182,7 @@ __device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int 
   for (int bi = threadIdx.x; bi < nb; bi += NT) {
     const int j = bi / NBX, i = bi - j * NBX;
     const int lx = OX + 2 * i, ly = ly0 + 2 * j;
+    if (!se_check(ly >= 0 && lx >= 0 && (ly + 1) * SW + lx + 1 < SW * SH, 2u)) continue;
     uint8_t* p = sm + ly * SW + lx;
     uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
     if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
@@ -254,6 +271,7 @@ __device__ __forceinline__ uint32_t se_lut_word_index(uint32_t abcd, uint32_t x)
   return se_gen::lut_index_key(key, h0, h1, h2, h3);
 }
 __device__ __forceinline__ uint32_t se_lut_fetch(const uint16_t* __restrict__ lut, uint32_t idx) {
+  if (!se_check(idx < SE_LUT_ENTRIES, 1u)) idx = 0;
 #if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
   return lut[idx];
 #else
@@ -266,16 +284,18 @@ __device__ __forceinline__ uint32_t se_lut_bytes(uint32_t o) {
   return (t | (t << 4)) & 0x0f0f0f0fu;
 }
 
-// Appends `entry` for the lanes with `dyn` set; every lane of the warp calls it.
+// Appends `entry` for the lanes with `dyn` set; every lane of the warp calls it.  The list
+// holds `cap` entries.
 __device__ __forceinline__ void se_list_push(bool dyn, uint32_t entry, uint16_t* __restrict__ list,
-                                             int* __restrict__ cnt) {
+                                             int* __restrict__ cnt, int cap) {
   const uint32_t m = __ballot_sync(0xffffffffu, dyn);
   if (m == 0u) return;
   const int lane = threadIdx.x & 31;
   int base = 0;
   if (lane == 0) base = atomicAdd(cnt, __popc(m));
   base = __shfl_sync(0xffffffffu, base, 0);
-  if (dyn) list[base + __popc(m & ((1u << lane) - 1u))] = (uint16_t)entry;
+  const int at = base + __popc(m & ((1u << lane) - 1u));
+  if (dyn && se_check(at < cap, 4u)) list[at] = (uint16_t)entry;
 }
 
 template <int SW, int SH, int OX, int NT>
@@ -285,6 +305,7 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int gx0, 
   static_assert(NT % 32 == 0 || NT == 1, "whole warps");
   static_assert(SW % 8 == 0 && SW * SH <= 65536, "8-byte rows, 16-bit offsets");
   constexpr int NBX = (SW - OX) / 2, NCX = NBX / 4, REM = NBX - 4 * NCX;
+  constexpr int CAP = (SW / 8) * (SH / 2);  // list capacity (tile_smem_bytes sizes it)
   const int nby = (SH - ly0) / 2;
   const int nc = NCX * nby;
   for (int base = threadIdx.x & ~31; base < nc; base += NT) {  // warp-uniform trip count
@@ -294,6 +315,8 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int gx0, 
     if (ci < nc) {
       const int j = ci / NCX, q = ci - j * NCX;
       off = (ly0 + 2 * j) * SW + OX + 8 * q;
+      // chunk loads at odd offsets read up to 3 bytes past the chunk: the 16-byte slack
+      if (!se_check(off >= 0 && off + SW + 11 <= ((SW * SH + 15) & ~15) + 16, 8u)) off = 0;
       uint32_t a0, a1, b0, b1;
       se_ld8<OX>(sm + off, a0, a1);
       se_ld8<OX>(sm + off + SW, b0, b1);
@@ -301,12 +324,13 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int gx0, 
       const bool uniform = ((a0 ^ a1) | (a0 ^ b0) | (a0 ^ b1)) == 0u && a0 == m * 0x01010101u;
       dyn = !(uniform && m < 16u && ((umask >> m) & 1u));
     }
-    se_list_push(dyn, (uint32_t)off, list, cnt);
+    se_list_push(dyn, (uint32_t)off, list, cnt, CAP);
   }
   if (REM) {  // blocks past the last whole chunk of each row
     for (int t = threadIdx.x; t < nby * REM; t += NT) {
       const int j = t / REM, r = t - j * REM;
       const int lx = OX + 2 * (4 * NCX + r), ly = ly0 + 2 * j;
+      if (!se_check((ly + 1) * SW + lx + 1 < SW * SH, 2u)) continue;
       uint8_t* p = sm + ly * SW + lx;
       uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
       if ((a | b | c | d) == 0u) continue;
@@ -338,12 +362,14 @@ __device__ __forceinline__ void se_chunk_eval(uint8_t* p, int SW, uint32_t x, co
   se_st8<OX>(p + SW, __byte_perm(B0, B1, 0x7632), __byte_perm(B2, B3, 0x7632));
 }
 
-template <int SW, int OX, int NT>
+template <int SW, int SH, int OX, int NT>
 __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int gx0,
                                                  int gy0, int f, const uint16_t* __restrict__ lut) {
   const uint32_t xf = (uint32_t)f * 4541161u;
   for (int i = threadIdx.x; i < n; i += NT) {
+    if (!se_check(i < (SW / 8) * (SH / 2), 4u)) break;
     const int off = list[i];
+    if (!se_check(off + SW + 11 <= ((SW * SH + 15) & ~15) + 16, 8u)) continue;
     const int ly = off / SW, lx = off - ly * SW;
     const uint32_t x = (uint32_t)(gx0 + lx) * 461u + (uint32_t)(gy0 + ly) * 2131u + xf;
     se_chunk_eval<OX>(sm + off, SW, x, lut);
@@ -369,6 +395,7 @@ __device__ __forceinline__ void se_step_rt(uint8_t* sm, int SW, int SH, int ox, 
       i += nbx;
     }
     const int lx = ox + 2 * i, ly = ly0 + 2 * j;
+    if (!se_check(ly >= 0 && lx >= 0 && (ly + 1) * SW + lx + 1 < SW * SH, 2u)) continue;
     uint8_t* p = sm + ly * SW + lx;
     uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
     if ((a | b | c | d) == 0u) continue;
@@ -424,7 +451,8 @@ __device__ __forceinline__ void se_load_region(uint8_t* sm, int SW, int SH, cons
         packed |= id << (8 * e);
       }
     }
-    *reinterpret_cast<uint32_t*>(sm + r * SW + 4 * c) = packed;
+    if (se_check(r >= 0 && r < SH && c >= 0 && c < wpr, 2u))
+      *reinterpret_cast<uint32_t*>(sm + r * SW + 4 * c) = packed;
   }
 }
 
@@ -447,6 +475,7 @@ __device__ __forceinline__ void se_store_region(const uint8_t* sm, int SW, int h
     }
     const int gy = Y0 + r, gx = X0 + 4 * c;
     if (gy >= H || gx >= W) continue;
+    if (!se_check(gy >= 0 && gx >= 0 && r >= 0 && c >= 0, 16u)) continue;
     const uint32_t packed = *reinterpret_cast<const uint32_t*>(sm + (r + hy) * SW + hx + 4 * c);
     if (vec && gx + 3 < W) {
       const uint4 v = make_uint4(packed & 0xffu, (packed >> 8) & 0xffu, (packed >> 16) & 0xffu, packed >> 24);
@@ -500,6 +529,10 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
         const int i = i0 + u * NT;
         if (i < NL) {
           const int r = i / WPR, c = i - r * WPR;
+          if (!se_check(gy0 - ya + r < yb - ya && gx0 + 4 * c + 3 < W, 16u)) {
+            v[u] = make_uint4(SE_WALL, SE_WALL, SE_WALL, SE_WALL);
+            continue;
+          }
           v[u] = __ldg(reinterpret_cast<const uint4*>(base + (size_t)r * W + 4 * c));
         }
       }
@@ -554,9 +587,9 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
       const int n = *c;
       if (threadIdx.x == 0) cnt[(s + 1) & 1] = 0;  // last read in step s - 1
       if (se_off_x(f) == 0)
-        se_chunk_process<SW, 0, NT>(sm, list, n, gx0, gy0, f, lut);
+        se_chunk_process<SW, SH, 0, NT>(sm, list, n, gx0, gy0, f, lut);
       else
-        se_chunk_process<SW, 1, NT>(sm, list, n, gx0, gy0, f, lut);
+        se_chunk_process<SW, SH, 1, NT>(sm, list, n, gx0, gy0, f, lut);
       __syncthreads();
       continue;
     }
@@ -573,6 +606,7 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
     const int r = i / OWPR, c = i - r * OWPR;
     const int gy = Y0 + r, gx = X0 + 4 * c;
     if (gy >= yb || gx >= W) continue;
+    if (!se_check(gy >= ya, 16u)) continue;
     const uint32_t packed = *reinterpret_cast<const uint32_t*>(sm + (r + HY) * SW + HX + 4 * c);
     uint32_t* out = dst + (size_t)(gy - ya) * W;
     if (vec && gx + 3 < W) {
@@ -735,5 +769,6 @@ extern "C" __global__ void __launch_bounds__(256) se_edit(uint32_t* __restrict__
   for (int r = q + 1; r < nmods; ++r)
     if (se_mod_hits(p.mods[r], x, y)) return;
   if (p.mods[q].mat == (int)SE_NULL) return;
-  grid[(size_t)(y - row0) * W + x] = (uint32_t)p.mods[q].mat;
+  if (se_check(y >= row0 && y < H && x >= 0 && x < W, 32u))  // H: the grid's last row + 1
+    grid[(size_t)(y - row0) * W + x] = (uint32_t)p.mods[q].mat;
 }

@@ -20,12 +20,29 @@ Status cuda_fail(const char* what, cudaError_t e) {
   } while (0)
 }  // namespace
 
+std::string Ruleset::device_source() const {
+  return (checked ? std::string("#define SE_CHECKED 1\n") : std::string()) + kernel_source(cuda.source);
+}
+
+Status Ruleset::check_word(unsigned int* word, bool reset) {
+  if (!checked) return {SE_ERR_INVALID_ARGUMENT, "the rule set was not compiled as a CHECKED build"};
+  Status s = ensure_loaded();
+  if (!s.ok()) return s;
+  void* p = nullptr;
+  size_t bytes = 0;
+  SE_CUDA(cudaLibraryGetGlobal(&p, &bytes, module->lib, "se_check_word"));
+  SE_CUDA(cudaDeviceSynchronize());
+  SE_CUDA(cudaMemcpy(word, p, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+  if (reset) SE_CUDA(cudaMemset(p, 0, sizeof(unsigned int)));
+  return Status::Ok();
+}
+
 Status Ruleset::compile() {
   std::lock_guard<std::mutex> g(mu);
   if (compiled) return Status::Ok();
   if (codegen_code) return {codegen_code, codegen_message};
   std::string log;
-  if (!compile_cubin(kernel_source(cuda.source), &cubin, &log)) return {SE_ERR_COMPILE, "NVRTC: " + log};
+  if (!compile_cubin(device_source(), &cubin, &log)) return {SE_ERR_COMPILE, "NVRTC: " + log};
   compiled = true;
   return Status::Ok();
 }

@@ -41,6 +41,11 @@ struct Ruleset {
   RenderMat* d_render = nullptr;
   ~Ruleset();
   LutShape lut_shape() const { return {cuda.lut_entries, cuda.lut_static_words}; }
+  // CHECKED build: the module is compiled with SE_CHECKED (index checks recorded in the
+  // device word se_check_word); set before the first compile.
+  bool checked = false;
+  std::string device_source() const;
+  Status check_word(unsigned int* word, bool reset);
   int num_materials() const { return (int)parsed.materials.size(); }
   Status compile();
   Status ensure_loaded();

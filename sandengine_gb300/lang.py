@@ -70,6 +70,16 @@ class Ruleset:
         check(lib().se_ruleset_material_id(self._h, name.encode(), ctypes.byref(i)))
         return i.value
 
+    def set_checked(self, enable: bool = True) -> None:
+        """CHECKED build: compile this rule set's kernels with index checks (before first use)."""
+        check(lib().se_ruleset_set_checked(self._h, 1 if enable else 0))
+
+    def check_word(self, reset: bool = True) -> int:
+        """Bits of the failed index checks of a CHECKED build since the last reset (0: none)."""
+        w = ctypes.c_uint(0)
+        check(lib().se_ruleset_check_word(self._h, ctypes.byref(w), 1 if reset else 0))
+        return w.value
+
     def table(self):
         """(table, static_bits) as built on the current CUDA device: the block transition
         table (u16 entries) and the bitset of static keys (u32 words), or (None, None) when

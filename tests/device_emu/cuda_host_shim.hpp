@@ -65,6 +65,11 @@ inline unsigned __ballot_sync(unsigned, bool p) { return p ? 1u : 0u; }
 template <class T>
 inline T __shfl_sync(unsigned, T v, int) { return v; }
 inline int __popc(unsigned v) { return __builtin_popcount(v); }
+inline unsigned atomicOr(unsigned* p, unsigned v) {
+  const unsigned old = *p;
+  *p = old | v;
+  return old;
+}
 inline int atomicAdd(int* p, int v) {
   const int old = *p;
   *p = old + v;

@@ -3,7 +3,9 @@
 Compiles the exact source handed to NVRTC (Ruleset.kernel_source) with g++ against
 cuda_host_shim.hpp and runs the tile kernels with one thread per CTA (see the shim's
 header) and the edit kernel thread by thread.  With ``lut=False`` the block transition
-table is compiled out, so the direct rule-evaluation path runs instead.
+table is compiled out, so the direct rule-evaluation path runs instead.  The source is
+compiled as the CHECKED build (SE_CHECKED): an emulated launch whose index checks fail
+raises.
 """
 import ctypes
 import hashlib
@@ -23,6 +25,16 @@ DRIVER = r'''
 alignas(16) uint8_t se_smem[1 << 21];
 static uint16_t* g_lut = nullptr;
 extern "C" const uint16_t* emu_lut() { return g_lut; }
+// the checker itself: one failed check of each kind (CPU self-test of the CHECKED build)
+extern "C" void emu_check_selftest() {
+  for (unsigned bit = 1; bit <= 32; bit <<= 1) (void)se_check(false, bit);
+}
+// index checks of the CHECKED build: failed-check bits since the last call, then cleared
+extern "C" unsigned emu_check_word() {
+  const unsigned w = se_check_word;
+  se_check_word = 0;
+  return w;
+}
 extern "C" uint32_t emu_lut_index_key(uint32_t i, uint32_t h0, uint32_t h1, uint32_t h2, uint32_t h3) {
 #ifdef SE_LUT
   return se_gen::lut_index_key(i, h0, h1, h2, h3);
@@ -115,6 +127,8 @@ class Emu:
         src = ruleset.kernel_source
         if not lut:
             src = src.replace("#define SE_LUT 1\n", "")
+        if "#define SE_CHECKED" not in src:  # every emulated launch runs the index checks
+            src = "#define SE_CHECKED 1\n" + src
         tiles = "\n".join(f"EMU_TILE({a}, {b}, {c})" for a, b, c in VARIANTS)
         mtiles = "\n".join(f"EMU_MTILE({a}, {b}, {c})" for a, b, c in VARIANTS)
         code = ('#include "cuda_host_shim.hpp"\n' + src +
@@ -137,8 +151,15 @@ class Emu:
                 raise RuntimeError(r.stderr[-4000:])
             os.replace(tmp, so)
         self.lib = ctypes.CDLL(so)
+        self.lib.emu_check_word.restype = ctypes.c_uint
         self.nmat = ruleset.num_materials
         self.has_lut = bool(self.lib.emu_build_lut())
+        self._checked()
+
+    def _checked(self):
+        w = self.lib.emu_check_word()
+        if w:
+            raise AssertionError(f"index check failed in the emulated kernel (check word {w:#x})")
 
     def tiles(self, src: np.ndarray, f0: int, k: int, variant=None, band=None) -> np.ndarray:
         """k frames (counters f0..f0+k-1) with one launch of the tile kernel.  With
@@ -151,6 +172,7 @@ class Emu:
         H, ya = band if band else (rows, 0)
         dst = np.zeros_like(src)
         fn(src.ctypes.data, dst.ctypes.data, W, H, f0, k, ya, ya + rows)
+        self._checked()
         return dst
 
     def batch(self, grids, frames0, F, k, resident, variant=(128, 64, 8)):
@@ -182,6 +204,7 @@ class Emu:
                 fn(desc.ctypes.data, jobs.ctypes.data, len(jobs), p, p * k, min(k, F - p * k))
         self.lib.emu_finalize.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         self.lib.emu_finalize(desc.ctypes.data, n, F, P)
+        self._checked()
         out = [bufs[i][int(desc[i]["cur"])] for i in range(n)]
         return out, [int(f) for f in desc["frame"]]
 
@@ -203,6 +226,7 @@ class Emu:
         pre = np.array(prefix, dtype=np.int32)
         self.lib.emu_stile_128x64_k8.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         self.lib.emu_stile_128x64_k8(desc.ctypes.data, pre.ctypes.data, n)
+        self._checked()
         return [o[1] for o in outs]
 
     def edit(self, grid: np.ndarray, mods) -> None:
@@ -234,3 +258,4 @@ class Emu:
             self.lib.emu_edit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_longlong, ctypes.c_void_p]
             self.lib.emu_edit(grid.ctypes.data, W, H, len(live), total, buf.ctypes.data)
+            self._checked()

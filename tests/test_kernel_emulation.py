@@ -218,3 +218,17 @@ def test_lut_index_classes_at_every_boundary(se, rulesets, name):
             for l in sorted(lanes):
                 want = want * (len(lanes[l]) + 1) + (sum(1 for t in lanes[l] if t <= hs[l]) if l == lane else 0)
             assert got == want, f"lane {lane} h={h:#x}: {got} != {want}"
+
+
+def test_checked_build_records_failed_checks(se, rulesets):
+    """The emulated kernels are the CHECKED build: se_check records failures in the check
+    word (read and cleared per launch by the emulator), so every emulated test above also
+    ran the index checks and none failed."""
+    E = Emu(se.parse_string(rulesets["four_materials"]), lut=True)
+    assert E.lib.emu_check_word() == 0
+    E.lib.emu_check_selftest()
+    assert E.lib.emu_check_word() == 0x3F
+    assert E.lib.emu_check_word() == 0  # cleared by the read
+    with pytest.raises(AssertionError):
+        E.lib.emu_check_selftest()
+        E._checked()
