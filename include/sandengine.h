@@ -308,6 +308,9 @@ int se_server_close_session(se_server* s, int session);
  * arrival_ms after the start of the next run.  Requests of one session run in order. */
 int se_server_submit(se_server* s, int session, int nframes, const se_modification* mods, int nmods,
                      double arrival_ms, int* request);
+/* Withdraws a submitted request that has not been run (cancelled before se_server_run):
+ * the run skips it, its session does not advance for it, and its latency query fails. */
+int se_server_cancel(se_server* s, int request);
 /* Serves every queued request in real time: requests are admitted when their arrival time
  * has passed and memory allows.  plain = 0: continuous batching (every active session
  * advances in one launch per iteration; sessions join and leave between iterations);

@@ -117,6 +117,7 @@ _SIGS = {
     "se_server_submit": ([_P, _I, _I, _P, _I, ctypes.c_double, ctypes.POINTER(_I)], _I),
     "se_server_run": ([_P, _I], _I),
     "se_server_stats_get": ([_P, _P], _I),
+    "se_server_cancel": ([_P, _I], _I),
     "se_server_request_latency": ([_P, _I, ctypes.POINTER(ctypes.c_double)], _I),
     "se_server_get_grid": ([_P, _I, _P, ctypes.c_size_t], _I),
     "se_server_get_frame": ([_P, _I, ctypes.POINTER(ctypes.c_int32)], _I),

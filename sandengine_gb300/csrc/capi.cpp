@@ -694,11 +694,19 @@ SE_API int se_server_stats_get(se_server* s, se_server_stats* out) {
   });
 }
 
+SE_API int se_server_cancel(se_server* s, int request) {
+  return guard([&] {
+    if (!s) return fail(SE_ERR_INVALID_ARGUMENT, "null server");
+    return ret(s->s->cancel(request));
+  });
+}
+
 SE_API int se_server_request_latency(se_server* s, int request, double* latency_ms) {
   return guard([&] {
     if (!s || !latency_ms || request < 0 || request >= (int)s->s->requests.size())
       return fail(SE_ERR_INVALID_ARGUMENT, "bad request");
     const auto& r = s->s->requests[(size_t)request];
+    if (r.cancelled) return fail(SE_ERR_INVALID_ARGUMENT, "request was cancelled");
     if (r.done_ms < 0) return fail(SE_ERR_INVALID_ARGUMENT, "request has not been served");
     *latency_ms = r.done_ms - r.arrival_ms;
     return (int)SE_OK;

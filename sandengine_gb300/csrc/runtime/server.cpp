@@ -116,13 +116,21 @@ Status Server::open_session(int w, int h, const uint32_t* cells, int32_t frame, 
   return Status::Ok();
 }
 
+Status Server::cancel(int request) {
+  if (request < (int)first_pending || request >= (int)requests.size())
+    return {SE_ERR_INVALID_ARGUMENT, "only a request that has not been run can be cancelled"};
+  requests[(size_t)request].cancelled = true;
+  return Status::Ok();
+}
+
 Status Server::close_session(int id) {
   if (id < 0 || id >= (int)sessions.size() || !sessions[(size_t)id].open)
     return {SE_ERR_INVALID_ARGUMENT, "bad session"};
   Session& s = sessions[(size_t)id];
   if (s.active >= 0 || !s.queue.empty()) return {SE_ERR_INVALID_ARGUMENT, "session has requests in flight"};
   for (size_t r = first_pending; r < requests.size(); ++r)
-    if (requests[r].session == id) return {SE_ERR_INVALID_ARGUMENT, "session has queued requests"};
+    if (requests[r].session == id && !requests[r].cancelled)
+      return {SE_ERR_INVALID_ARGUMENT, "session has queued requests"};
   if (s.resident) {
     SE_CUDA(cudaStreamSynchronize(stream));
     release(s.off, s.bytes);
@@ -240,7 +248,8 @@ Status Server::run(bool plain) {
 Status Server::run_batched() {
   TraceRange trace("se_server_run_batched");
   std::vector<int> pend;
-  for (size_t i = first_pending; i < requests.size(); ++i) pend.push_back((int)i);
+  for (size_t i = first_pending; i < requests.size(); ++i)
+    if (!requests[i].cancelled) pend.push_back((int)i);
   std::stable_sort(pend.begin(), pend.end(),
                    [&](int a, int b) { return requests[(size_t)a].arrival_ms < requests[(size_t)b].arrival_ms; });
   cudaEvent_t t0;
@@ -386,7 +395,8 @@ Status Server::run_batched() {
 Status Server::run_plain() {
   TraceRange trace("se_server_run_plain");
   std::vector<int> pend;
-  for (size_t i = first_pending; i < requests.size(); ++i) pend.push_back((int)i);
+  for (size_t i = first_pending; i < requests.size(); ++i)
+    if (!requests[i].cancelled) pend.push_back((int)i);
   std::stable_sort(pend.begin(), pend.end(),
                    [&](int a, int b) { return requests[(size_t)a].arrival_ms < requests[(size_t)b].arrival_ms; });
   const TileVariant* v1 = nullptr;

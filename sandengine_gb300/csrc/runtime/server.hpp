@@ -37,6 +37,7 @@ struct Server {
     std::vector<se_modification> mods;
     double arrival_ms = 0;
     bool started = false;
+    bool cancelled = false;  // withdrawn before it started (se_server_cancel)
     long long iter = -1;  // iteration that completed it
     double done_ms = -1;
   };
@@ -73,6 +74,9 @@ struct Server {
   Status open_session(int w, int h, const uint32_t* cells, int32_t frame, int* id);
   Status close_session(int id);
   Status submit(int session, int nframes, const se_modification* mods, int nmods, double arrival_ms, int* id);
+  // Withdraws a request that has not been run yet: the next run skips it and its session's
+  // frame counter does not move for it.
+  Status cancel(int request);
   Status run(bool plain);
   Status get_grid(int session, uint32_t* host, size_t count);
   Status stats(se_server_stats* out);

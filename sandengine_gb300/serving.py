@@ -75,6 +75,10 @@ class Server:
                                      float(arrival_ms), ctypes.byref(rid)))
         return rid.value
 
+    def cancel(self, request: int) -> None:
+        """Withdraw a request that has not been run yet."""
+        check(lib().se_server_cancel(self._h, int(request)))
+
     def run(self, plain: bool = False) -> None:
         check(lib().se_server_run(self._h, 1 if plain else 0))
 

@@ -97,3 +97,38 @@ def test_session_larger_than_budget_is_rejected(se, rulesets):
     with pytest.raises(se.SandengineError) as e:
         srv.open_session(1024, 1024)
     assert e.value.kind == "Budget"
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_cancelled_requests_are_skipped(se, ports, rulesets, plain):
+    """Host-side fault injection: requests withdrawn before the run are skipped (their
+    sessions do not advance for them), the others are served exactly; a request that has
+    run cannot be cancelled, and a cancelled one has no latency."""
+    from sandengine_gb300 import workloads as wl
+    from sandengine_gb300.serving import Server
+    rs = se.parse_string(rulesets["twelve_materials"])
+    P = ports["twelve_materials"]
+    sizes = [(200, 150), (64, 64), (333, 120)]
+    grids = [wl.patch_fill(w, h, 70 + i, *wl.twelve_fill_spec(), patch=16) for i, (w, h) in enumerate(sizes)]
+    srv = Server(rs, 1 << 30)
+    sids = [srv.open_session(w, h, g, 3) for (w, h), g in zip(sizes, grids)]
+    plan = [(0, 10), (1, 7), (2, 12), (0, 5), (1, 9), (2, 4)]
+    rids = [srv.submit(s, n) for s, n in plan]
+    cancelled = {rids[1], rids[3], rids[5]}
+    for r in cancelled:
+        srv.cancel(r)
+    srv.run(plain=plain)
+    frames = [3, 3, 3]
+    for r, (s, n) in zip(rids, plan):
+        if r in cancelled:
+            continue
+        P.run(grids[s], frames[s], n)
+        frames[s] += n
+    for s in sids:
+        assert np.array_equal(srv.grid(s), grids[s]), f"session {s}"
+        assert srv.frame(s) == frames[s]
+    with pytest.raises(se.SandengineError):
+        srv.cancel(rids[0])  # already run
+    with pytest.raises(se.SandengineError):
+        srv.latency_ms(rids[1])  # cancelled
+    assert srv.latency_ms(rids[0]) >= 0
