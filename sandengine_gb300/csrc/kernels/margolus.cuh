@@ -192,16 +192,19 @@ __device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int 
   }
 }
 
-#ifdef SE_LUT
-// Interior tiles with a block transition table run each step in two phases over chunks of
-// four horizontally adjacent blocks (8 cells x 2 rows):
+#ifndef SE_LUT
+#define SE_LUT_SMEM_BYTES 0u
+#endif
+// Interior tiles run each step in two phases over chunks of four horizontally adjacent
+// blocks (8 cells x 2 rows):
 //  1. se_chunk_collect reads every chunk with two 8-byte loads.  A chunk whose 16 cells are
-//     one material m, where the table never changes the block of four m cells (EMPTY, and
-//     in a typical rule set the solids and liquids at rest), is left as it is; the others
-//     are appended to a list of array offsets (a warp reserves its slots with one
-//     atomicAdd).  The blocks of a row past its last whole chunk are updated right there.
-//  2. se_chunk_process updates the listed chunks, one chunk per thread, with word-wide
-//     shared-memory access.
+//     one material m whose block of four m cells never changes is left as it is (with a
+//     transition table: EMPTY, and in a typical rule set the solids and liquids at rest;
+//     without one: EMPTY, which the shader itself leaves alone); the others are appended
+//     to a list of array offsets (a warp reserves its slots with one atomicAdd).  The
+//     blocks of a row past its last whole chunk are updated right there.
+//  2. se_chunk_process updates the listed chunks, one chunk per thread: with a table
+//     word-wide and with four independent lookups, else block by block with the rules.
 // Chunks are skipped whole, so the lanes that evaluate blocks do so together rather than
 // waiting on one another; blocks of one step are disjoint, so the list order is free.
 
@@ -212,15 +215,21 @@ __device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int 
 #define SE_HDR_FLAGS 32
 #define SE_HDR_LIST 48
 
-// flags[m] = 1 when the block of four m cells is static (from se_build_static's bitset).
+// flags[m] = 1 when the block of four m cells is static: from se_build_static's bitset
+// with a transition table, else EMPTY only.
 __device__ __forceinline__ void se_uniform_flags(const uint16_t* __restrict__ lut, uint8_t* flags, int nt) {
+#ifdef SE_LUT
   const uint32_t* st = reinterpret_cast<const uint32_t*>(reinterpret_cast<const uint8_t*>(lut) + SE_LUT_STATIC_OFF);
+#endif
   for (uint32_t m = threadIdx.x; m < 16u; m += nt) {
-    uint32_t bit = 0;
+    uint32_t bit = m == 0u;
+#ifdef SE_LUT
+    bit = 0;
     if (m < SE_NMAT && m < (1u << SE_LUT_BITS)) {
       const uint32_t key = se_gen::lut_key(m, m, m, m);
       bit = (__ldg(st + (key >> 5)) >> (key & 31u)) & 1u;
     }
+#endif
     flags[m] = (uint8_t)bit;
   }
 }
@@ -259,6 +268,7 @@ __device__ __forceinline__ void se_st8(uint8_t* p, uint32_t lo, uint32_t hi) {
   }
 }
 
+#ifdef SE_LUT
 // Table index of a block given as the 4 bytes [a, b, c, d] (ids < 16) with hash base x.
 __device__ __forceinline__ uint32_t se_lut_word_index(uint32_t abcd, uint32_t x) {
 #if SE_LUT_BITS == 4
@@ -283,6 +293,7 @@ __device__ __forceinline__ uint32_t se_lut_bytes(uint32_t o) {
   const uint32_t t = (o & 0xffu) | ((o << 8) & 0xff0000u);
   return (t | (t << 4)) & 0x0f0f0f0fu;
 }
+#endif
 
 // Appends `entry` for the lanes with `dyn` set; every lane of the warp calls it.  The list
 // holds `cap` entries.
@@ -341,6 +352,7 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int gx0, 
   }
 }
 
+#ifdef SE_LUT
 // Updates the chunk (4 blocks, 8 x 2 cells) at p, row stride SW, whose first block's hash
 // base is x, with word-wide shared-memory access.
 template <int OX>
@@ -361,21 +373,35 @@ __device__ __forceinline__ void se_chunk_eval(uint8_t* p, int SW, uint32_t x, co
   se_st8<OX>(p, __byte_perm(B0, B1, 0x5410), __byte_perm(B2, B3, 0x5410));
   se_st8<OX>(p + SW, __byte_perm(B0, B1, 0x7632), __byte_perm(B2, B3, 0x7632));
 }
+#endif
 
 template <int SW, int SH, int OX, int NT>
 __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int gx0,
-                                                 int gy0, int f, const uint16_t* __restrict__ lut) {
+                                                 int gy0, int f, int W, int H, const uint16_t* __restrict__ lut) {
   const uint32_t xf = (uint32_t)f * 4541161u;
   for (int i = threadIdx.x; i < n; i += NT) {
     if (!se_check(i < (SW / 8) * (SH / 2), 4u)) break;
     const int off = list[i];
     if (!se_check(off + SW + 11 <= ((SW * SH + 15) & ~15) + 16, 8u)) continue;
     const int ly = off / SW, lx = off - ly * SW;
+#ifdef SE_LUT
     const uint32_t x = (uint32_t)(gx0 + lx) * 461u + (uint32_t)(gy0 + ly) * 2131u + xf;
     se_chunk_eval<OX>(sm + off, SW, x, lut);
+#else
+    (void)xf;
+    for (int kb = 0; kb < 4; ++kb) {  // the generated rules, block by block
+      uint8_t* p = sm + off + 2 * kb;
+      uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+      if ((a | b | c | d) == 0u) continue;
+      se_block(a, b, c, d, gx0 + lx + 2 * kb, gy0 + ly, f, W, H);
+      p[0] = (uint8_t)a;
+      p[1] = (uint8_t)b;
+      p[SW] = (uint8_t)c;
+      p[SW + 1] = (uint8_t)d;
+    }
+#endif
   }
 }
-#endif
 
 // The same over a shared array whose size is only known at run time (whole worlds); the
 // block index is split with a float reciprocal and a +-1 correction.
@@ -505,14 +531,12 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   extern __shared__ __align__(16) uint8_t se_smem[];
   uint8_t* sm = se_smem;
   se_gen::init_tables(threadIdx.x, NT);
-#ifdef SE_LUT
   constexpr int HDR = ((SW * SH + 15) & ~15) + (int)SE_LUT_SMEM_BYTES;
   int* cnt = reinterpret_cast<int*>(se_smem + HDR + SE_HDR_CNT);
   uint8_t* flags = se_smem + HDR + SE_HDR_FLAGS;
   uint16_t* list = reinterpret_cast<uint16_t*>(se_smem + HDR + SE_HDR_LIST);
   for (int i = threadIdx.x; i < 2; i += NT) cnt[i] = 0;
   se_uniform_flags(lut, flags, NT);
-#endif
   lut = se_lut_to_smem(lut, se_smem, (SW * SH + 15) & ~15, NT);
   const int gx0 = X0 - HX, gy0 = Y0 - HY;
   const bool vec = (W & 3) == 0;
@@ -570,13 +594,10 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   __syncthreads();
 
   const bool edge = gx0 < 0 || gy0 < 0 || gx0 + SW > W || gy0 + SH > H;
-#ifdef SE_LUT
   const uint32_t umask = se_flags_mask(flags);
-#endif
   for (int s = 0; s < k; ++s) {
     const int f = f0 + s;
     const int ly0 = (se_off_y(f) + gy0) & 1;  // gy0 = Y0 - HY is odd when HY is
-#ifdef SE_LUT
     if (!edge) {
       int* c = cnt + (s & 1);
       if (se_off_x(f) == 0)
@@ -587,13 +608,12 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
       const int n = *c;
       if (threadIdx.x == 0) cnt[(s + 1) & 1] = 0;  // last read in step s - 1
       if (se_off_x(f) == 0)
-        se_chunk_process<SW, SH, 0, NT>(sm, list, n, gx0, gy0, f, lut);
+        se_chunk_process<SW, SH, 0, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
       else
-        se_chunk_process<SW, SH, 1, NT>(sm, list, n, gx0, gy0, f, lut);
+        se_chunk_process<SW, SH, 1, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
       __syncthreads();
       continue;
     }
-#endif
     if (se_off_x(f) == 0)
       se_tile_step<SW, SH, 0, NT>(sm, ly0, gx0, gy0, f, W, H, edge, lut);
     else

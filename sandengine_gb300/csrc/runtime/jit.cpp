@@ -165,9 +165,9 @@ size_t lut_smem_bytes(const LutShape& lut) {
 
 size_t tile_smem_bytes(const TileVariant& t, const LutShape& lut) {
   size_t b = ((t.smem_bytes() + 15) & ~(size_t)15) + lut_smem_bytes(lut);
-  // with a table: 48-byte header (slack, list counters, uniform-material flags), then the
-  // per-step list of chunks (4 blocks) to evaluate, one u16 offset each
-  if (lut.entries) b += 48 + ((2 * (size_t)(t.sw() / 8) * (size_t)(t.sh() / 2) + 15) & ~(size_t)15);
+  // 48-byte header (slack, list counters, uniform-material flags), then the per-step list
+  // of chunks (4 blocks) to evaluate, one u16 offset each
+  b += 48 + ((2 * (size_t)(t.sw() / 8) * (size_t)(t.sh() / 2) + 15) & ~(size_t)15);
   return b;
 }
 

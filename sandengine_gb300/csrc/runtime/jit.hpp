@@ -36,8 +36,8 @@ struct LutShape {
 // Shared memory the table copy of a CTA takes (the table when it fits, rounded up to 16
 // bytes).  The static-key bitset stays in global memory.
 size_t lut_smem_bytes(const LutShape& lut);
-// Dynamic shared memory of a tile launch: the u8 tile, then the table copy, then (with a
-// table) the per-step list of chunks to evaluate.
+// Dynamic shared memory of a tile launch: the u8 tile, then the table copy, then the
+// per-step list of chunks to evaluate.
 size_t tile_smem_bytes(const TileVariant& t, const LutShape& lut);
 
 // Full device source: prelude + generated rules + kernel template + instantiations.
