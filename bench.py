@@ -317,7 +317,10 @@ def run_ours(args, rep):
         "gpu_launches": launches + args.steps + sum(p["launches"] for p in passes.values()),
         "clocks": clocks.summary(),
     }
-    for p, name, bpc in ((1, "light_pass", 40.0), (2, "color_pass", 24.0), (3, "composite_pass", 48.0)):
+    # algorithmic bytes per cell: light = old id, new id, old light in, light out (4 + 4 + 16 + 16);
+    # colour (inside the composite) = id, noise, RGBA out and a quarter of the level-1 alpha
+    # float; composite = colour, light, RGBA out (the smaller pyramid levels are not counted)
+    for p, name, bpc in ((1, "light_pass", 40.0), (2, "color_pass", 25.0), (3, "composite_pass", 48.0)):
         if p in passes and passes[p]["launches"]:
             t = passes[p]
             avg_s = t["kernel_ms"] / t["launches"] / 1e3

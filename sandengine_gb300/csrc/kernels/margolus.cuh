@@ -269,16 +269,14 @@ __device__ __forceinline__ void se_st8(uint8_t* p, uint32_t lo, uint32_t hi) {
 }
 
 #ifdef SE_LUT
-// Table index of a block given as the 4 bytes [a, b, c, d] (ids < 16) with hash base x.
-__device__ __forceinline__ uint32_t se_lut_word_index(uint32_t abcd, uint32_t x) {
-#if SE_LUT_BITS == 4
-  const uint32_t y = abcd | (abcd >> 4);  // byte 0 = a | b << 4, byte 2 = c | d << 4
-  const uint32_t key = (y & 0xffu) | ((y >> 8) & 0xff00u);
-#else
-  const uint32_t key = se_gen::lut_key(abcd & 0xffu, (abcd >> 8) & 0xffu, (abcd >> 16) & 0xffu, abcd >> 24);
-#endif
+// Table index of a block's key with hash base x.
+__device__ __forceinline__ uint32_t se_lut_key_index(uint32_t key, uint32_t x) {
   const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u), h3 = se_mix(x * 213132u);
   return se_gen::lut_index_key(key, h0, h1, h2, h3);
+}
+// Table index of a block given as the 4 bytes [a, b, c, d] (ids < 16) with hash base x.
+__device__ __forceinline__ uint32_t se_lut_word_index(uint32_t abcd, uint32_t x) {
+  return se_lut_key_index(se_gen::lut_key(abcd & 0xffu, (abcd >> 8) & 0xffu, (abcd >> 16) & 0xffu, abcd >> 24), x);
 }
 __device__ __forceinline__ uint32_t se_lut_fetch(const uint16_t* __restrict__ lut, uint32_t idx) {
   if (!se_check(idx < SE_LUT_ENTRIES, 1u)) idx = 0;
@@ -287,11 +285,6 @@ __device__ __forceinline__ uint32_t se_lut_fetch(const uint16_t* __restrict__ lu
 #else
   return __ldg(lut + idx);
 #endif
-}
-// A table entry (nibbles a | b << 4 | c << 8 | d << 12) as the 4 bytes [a, b, c, d].
-__device__ __forceinline__ uint32_t se_lut_bytes(uint32_t o) {
-  const uint32_t t = (o & 0xffu) | ((o << 8) & 0xff0000u);
-  return (t | (t << 4)) & 0x0f0f0f0fu;
 }
 #endif
 
@@ -360,18 +353,33 @@ __device__ __forceinline__ void se_chunk_eval(uint8_t* p, int SW, uint32_t x, co
   uint32_t a0, a1, b0, b1;
   se_ld8<OX>(p, a0, a1);
   se_ld8<OX>(p + SW, b0, b1);
-  // [a, b, c, d] of the four blocks; block origins are 2 cells apart (x + 922 each).  No
-  // branch on all-EMPTY blocks (the table maps them to themselves), so the four lookups are
-  // in flight together.
+  // The four blocks' keys; block origins are 2 cells apart (x + 922 each).  No branch on
+  // all-EMPTY blocks (the table maps them to themselves), so the four lookups are in flight
+  // together.
+#if SE_LUT_BITS == 4
+  // A row word holds 4 cells (< 16 each); in w | w >> 4, byte 0 is the left block's
+  // left | right << 4 and byte 2 the right block's, so one permute of the two rows' words
+  // gives both blocks' keys (key0 | key1 << 16).
+  const uint32_t k01 = __byte_perm(a0 | (a0 >> 4), b0 | (b0 >> 4), 0x6240);
+  const uint32_t k23 = __byte_perm(a1 | (a1 >> 4), b1 | (b1 >> 4), 0x6240);
+  const uint32_t i0 = se_lut_key_index(k01 & 0xffffu, x), i1 = se_lut_key_index(k01 >> 16, x + 922u);
+  const uint32_t i2 = se_lut_key_index(k23 & 0xffffu, x + 1844u), i3 = se_lut_key_index(k23 >> 16, x + 2766u);
+#else
   const uint32_t i0 = se_lut_word_index(__byte_perm(a0, b0, 0x5410), x);
   const uint32_t i1 = se_lut_word_index(__byte_perm(a0, b0, 0x7632), x + 922u);
   const uint32_t i2 = se_lut_word_index(__byte_perm(a1, b1, 0x5410), x + 1844u);
   const uint32_t i3 = se_lut_word_index(__byte_perm(a1, b1, 0x7632), x + 2766u);
+#endif
   const uint32_t o0 = se_lut_fetch(lut, i0), o1 = se_lut_fetch(lut, i1), o2 = se_lut_fetch(lut, i2),
                  o3 = se_lut_fetch(lut, i3);
-  const uint32_t B0 = se_lut_bytes(o0), B1 = se_lut_bytes(o1), B2 = se_lut_bytes(o2), B3 = se_lut_bytes(o3);
-  se_st8<OX>(p, __byte_perm(B0, B1, 0x5410), __byte_perm(B2, B3, 0x5410));
-  se_st8<OX>(p + SW, __byte_perm(B0, B1, 0x7632), __byte_perm(B2, B3, 0x7632));
+  // Entries are nibbles a | b << 4 | c << 8 | d << 12.  Two blocks' entries side by side,
+  // split into even and odd nibbles, permute into the top row [a, b, a', b'] and the
+  // bottom row [c, d, c', d'].
+  const uint32_t P01 = __byte_perm(o0, o1, 0x5410), P23 = __byte_perm(o2, o3, 0x5410);
+  const uint32_t E01 = P01 & 0x0f0f0f0fu, O01 = (P01 >> 4) & 0x0f0f0f0fu;
+  const uint32_t E23 = P23 & 0x0f0f0f0fu, O23 = (P23 >> 4) & 0x0f0f0f0fu;
+  se_st8<OX>(p, __byte_perm(E01, O01, 0x6240), __byte_perm(E23, O23, 0x6240));
+  se_st8<OX>(p + SW, __byte_perm(E01, O01, 0x7351), __byte_perm(E23, O23, 0x7351));
 }
 #endif
 
