@@ -89,6 +89,58 @@ __global__ void __launch_bounds__(256) se_color_kernel(const uint32_t* __restric
   }
 }
 
+// The colour of one cell and its alpha.
+__device__ __forceinline__ float4 cell_color(uint32_t id, float nz, const RenderMat* __restrict__ mats, int nmat) {
+  const RenderMat* r = mats + mat_index(id, nmat);
+  float4 c = make_float4(__ldg(r->color + 0), __ldg(r->color + 1), __ldg(r->color + 2), __ldg(r->color + 3));
+  if (__ldg(&r->flags) & kRenderNoise) {
+    const float d = fmul(nz, 0.25f);
+    c.x = gclamp(fsub(c.x, d), 0.0f, 1.0f);
+    c.y = gclamp(fsub(c.y, d), 0.0f, 1.0f);
+    c.z = gclamp(fsub(c.z, d), 0.0f, 1.0f);
+  }
+  return c;
+}
+
+// Thread = cells (2x, 2y) .. (2x + 1, 2y + 1): their colours, and (alpha1 != null, x < dw,
+// y < dh) the level-1 alpha ((a00 + a10) + a01 + a11) * 0.25 in the mip kernel's order.
+// At an odd last row or column the pair's second index is clamped, as the mip's is.
+__global__ void __launch_bounds__(256) se_color_mip_kernel(const uint32_t* __restrict__ grid,
+                                                           const float* __restrict__ noise, float4* __restrict__ out,
+                                                           float* __restrict__ alpha1, int W, int H, int dw, int dh,
+                                                           const RenderMat* __restrict__ mats, int nmat) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int c0 = 2 * x, r0 = 2 * y;
+  if (c0 >= W || r0 >= H) return;
+  const bool pair = c0 + 1 < W;
+  float a[2][2];
+#pragma unroll
+  for (int dr = 0; dr < 2; ++dr) {
+    const int r = min(r0 + dr, H - 1);
+    const size_t i = (size_t)r * W + c0;
+    uint32_t id0, id1;
+    float n0, n1;
+    if (pair && (W & 1) == 0) {  // 8-byte aligned pairs
+      const uint2 g = __ldg(reinterpret_cast<const uint2*>(grid + i));
+      const float2 z = __ldg(reinterpret_cast<const float2*>(noise + i));
+      id0 = g.x, id1 = g.y, n0 = z.x, n1 = z.y;
+    } else {
+      id0 = __ldg(grid + i), n0 = __ldg(noise + i);
+      id1 = pair ? __ldg(grid + i + 1) : id0;
+      n1 = pair ? __ldg(noise + i + 1) : n0;
+    }
+    const float4 k0 = cell_color(id0, n0, mats, nmat), k1 = cell_color(id1, n1, mats, nmat);
+    if (r == r0 + dr) {
+      out[i] = k0;
+      if (pair) out[i + 1] = k1;
+    }
+    a[dr][0] = k0.w;
+    a[dr][1] = k1.w;
+  }
+  if (alpha1 && x < dw && y < dh)
+    alpha1[(size_t)y * dw + x] = fmul(fadd(fadd(fadd(a[0][0], a[0][1]), a[1][0]), a[1][1]), 0.25f);
+}
+
 // Light pass over a 64 x 16 tile per CTA.  The tile plus a one-cell ring is staged in
 // shared memory as each cell's contribution to its neighbours' blend,
 // (rgb * keep * a, a) for its previous light (rgb, a), where keep is 0 when its old cell is a
@@ -235,8 +287,14 @@ __device__ float4 sample_linear(const float4* t, int w, int h, float u, float v)
   const float fx = floorf(x), fy = floorf(y);
   const float a = fsub(x, fx), b = fsub(y, fy);
   const int i = (int)fx, j = (int)fy;
-  const float4 t00 = tap(t, w, h, i, j), t10 = tap(t, w, h, i + 1, j), t01 = tap(t, w, h, i, j + 1),
-               t11 = tap(t, w, h, i + 1, j + 1);
+  float4 t00, t10, t01, t11;
+  if ((unsigned)i < (unsigned)(w - 1) && (unsigned)j < (unsigned)(h - 1)) {  // all four taps inside: no wrap
+    const float4* p = t + (size_t)j * w + i;
+    t00 = __ldg(p), t10 = __ldg(p + 1), t01 = __ldg(p + w), t11 = __ldg(p + w + 1);
+  } else {
+    t00 = tap(t, w, h, i, j), t10 = tap(t, w, h, i + 1, j), t01 = tap(t, w, h, i, j + 1),
+    t11 = tap(t, w, h, i + 1, j + 1);
+  }
   const float w00 = fmul(fsub(1.0f, a), fsub(1.0f, b)), w10 = fmul(a, fsub(1.0f, b)), w01 = fmul(fsub(1.0f, a), b),
               w11 = fmul(a, b);
   return make_float4(lerp4(t00.x, t10.x, t01.x, t11.x, w00, w10, w01, w11),
@@ -244,36 +302,47 @@ __device__ float4 sample_linear(const float4* t, int w, int h, float u, float v)
                      lerp4(t00.z, t10.z, t01.z, t11.z, w00, w10, w01, w11),
                      lerp4(t00.w, t10.w, t01.w, t11.w, w00, w10, w01, w11));
 }
-// textureLod with MAG NEAREST / MIN LINEAR_MIPMAP_NEAREST, alpha only
-__device__ float sample_lod_alpha(const MipChain& m, float u, float v, float lod) {
-  if (lod <= 0.0f) return sample_nearest(m.level[0], m.w[0], m.h[0], u, v).w;
-  int d = lod <= 0.5f ? 0 : (int)ceilf(fadd(lod, 0.5f)) - 1;
-  if (d > m.n - 1) d = m.n - 1;
-  return sample_linear(m.level[d], m.w[d], m.h[d], u, v).w;
+// One channel of a texture whose texel (i, j) is t[S * (j * w + i)]: S = 4 reads the
+// alpha of an RGBA level, S = 1 an alpha level.  4-byte taps.
+template <int S>
+__device__ __forceinline__ float tap_a(const float* t, int w, int h, int i, int j) {
+  return __ldg(t + (size_t)S * ((size_t)mirror_index(j, h) * w + mirror_index(i, w)));
 }
-// sampleBlurred(tex, uv, radius, gamma).a with lod = log2(radius)
-__device__ float blurred_alpha(const MipChain& m, float u, float v, float lod, float w_side) {
-  float acc = 0.0f, wsum = 0.0f;
-#pragma unroll
-  for (int k = -1; k <= 1; ++k) {
-    const float w = k == 0 ? 1.0f : w_side;  // exp(-gamma * pow(lod - i, 2))
-    acc = fadd(acc, fmul(sample_lod_alpha(m, u, v, fadd(lod, (float)k)), w));
-    wsum = fadd(wsum, w);
+template <int S>
+__device__ float sample_linear_a(const float* t, int w, int h, float u, float v) {
+  const float x = fsub(fmul(u, (float)w), 0.5f), y = fsub(fmul(v, (float)h), 0.5f);
+  const float fx = floorf(x), fy = floorf(y);
+  const float a = fsub(x, fx), b = fsub(y, fy);
+  const int i = (int)fx, j = (int)fy;
+  float t00, t10, t01, t11;
+  if ((unsigned)i < (unsigned)(w - 1) && (unsigned)j < (unsigned)(h - 1)) {  // all four taps inside: no wrap
+    const float* p = t + (size_t)S * ((size_t)j * w + i);
+    t00 = __ldg(p), t10 = __ldg(p + S), t01 = __ldg(p + (size_t)S * w), t11 = __ldg(p + (size_t)S * w + S);
+  } else {
+    t00 = tap_a<S>(t, w, h, i, j), t10 = tap_a<S>(t, w, h, i + 1, j), t01 = tap_a<S>(t, w, h, i, j + 1),
+    t11 = tap_a<S>(t, w, h, i + 1, j + 1);
   }
-  return __fdiv_rn(acc, wsum);
+  const float w00 = fmul(fsub(1.0f, a), fsub(1.0f, b)), w10 = fmul(a, fsub(1.0f, b)), w01 = fmul(fsub(1.0f, a), b),
+              w11 = fmul(a, b);
+  return lerp4(t00, t10, t01, t11, w00, w10, w01, w11);
+}
+// sampleBlurred(tex, uv, radius, gamma).a with lod = log2(radius), from its three textureLod
+// samples at lod - 1, lod, lod + 1: weights exp(-gamma * (lod - i)^2) = w_side, 1, w_side.
+__device__ __forceinline__ float blurred_alpha(float lo, float mid, float hi, float w_side) {
+  float acc = fadd(0.0f, fmul(lo, w_side));
+  acc = fadd(acc, fmul(mid, 1.0f));
+  acc = fadd(acc, fmul(hi, w_side));
+  return __fdiv_rn(acc, fadd(fadd(fadd(0.0f, w_side), 1.0f), w_side));
 }
 
-__global__ void __launch_bounds__(256) se_mip_kernel(const float4* __restrict__ src, int sw, int sh,
-                                                     float4* __restrict__ dst, int dw, int dh) {
+__global__ void __launch_bounds__(256) se_mip_alpha_kernel(const float* __restrict__ src, int sw, int sh,
+                                                           float* __restrict__ dst, int dw, int dh) {
   const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
   if (x >= dw || y >= dh) return;
   const int x0 = min(2 * x, sw - 1), x1 = min(2 * x + 1, sw - 1), y0 = min(2 * y, sh - 1), y1 = min(2 * y + 1, sh - 1);
-  const float4 a = __ldg(src + (size_t)y0 * sw + x0), b = __ldg(src + (size_t)y0 * sw + x1),
-               c = __ldg(src + (size_t)y1 * sw + x0), d = __ldg(src + (size_t)y1 * sw + x1);
-  dst[(size_t)y * dw + x] = make_float4(fmul(fadd(fadd(fadd(a.x, b.x), c.x), d.x), 0.25f),
-                                        fmul(fadd(fadd(fadd(a.y, b.y), c.y), d.y), 0.25f),
-                                        fmul(fadd(fadd(fadd(a.z, b.z), c.z), d.z), 0.25f),
-                                        fmul(fadd(fadd(fadd(a.w, b.w), c.w), d.w), 0.25f));
+  const float a = __ldg(src + (size_t)y0 * sw + x0), b = __ldg(src + (size_t)y0 * sw + x1),
+              c = __ldg(src + (size_t)y1 * sw + x0), d = __ldg(src + (size_t)y1 * sw + x1);
+  dst[(size_t)y * dw + x] = fmul(fadd(fadd(fadd(a, b), c), d), 0.25f);
 }
 
 // The part of a fragment that depends only on the pixelated coordinate (pu, pv): the
@@ -281,26 +350,33 @@ __global__ void __launch_bounds__(256) se_mip_kernel(const float4* __restrict__ 
 struct Shared {
   float lr, lg, lb, occ;
 };
-__device__ Shared shared_terms(const MipChain& m, const float4* __restrict__ light, float pu, float pv, float ws0,
+__device__ Shared shared_terms(const CompositeSrc& m, const float4* __restrict__ light, float pu, float pv, float ws0,
                                float ws1, float ws2) {
-  float4 li = light ? sample_linear(light, m.w[0], m.h[0], pu, pv) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  float occ = fsub(1.0f, blurred_alpha(m, pu, pv, 1.0f, ws0));
-  const float occ2 = fsub(1.0f, blurred_alpha(m, pu, pv, 4.0f, ws1));
-  const float occ3 = fsub(1.0f, blurred_alpha(m, pu, pv, 5.0f, ws2));
+  float4 li = light ? sample_linear(light, m.w, m.h, pu, pv) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  // The three sampleBlurred calls (lod 1, 4, 5) take textureLod at lods 0..2, 3..5 and 4..6:
+  // seven distinct samples.  lod 0 is a magnification (level 0, nearest); lod l >= 1 reads
+  // the alpha level in slot l, bilinearly.
+  const float s0 = tap_a<4>(&m.color->w, m.w, m.h, (int)floorf(fmul(pu, (float)m.w)), (int)floorf(fmul(pv, (float)m.h)));
+  float s[kOccLods];
+#pragma unroll
+  for (int l = 1; l < kOccLods; ++l) s[l] = sample_linear_a<1>(m.alpha[l], m.aw[l], m.ah[l], pu, pv);
+  float occ = fsub(1.0f, blurred_alpha(s0, s[1], s[2], ws0));
+  const float occ2 = fsub(1.0f, blurred_alpha(s[3], s[4], s[5], ws1));
+  const float occ3 = fsub(1.0f, blurred_alpha(s[4], s[5], s[6], ws2));
   occ = gclamp(fadd(occ, fadd(fmul(occ2, 0.4f), fmul(occ3, 0.25f))), 0.0f, 1.0f);
   return Shared{gclamp(li.x, 0.0f, 1.0f), gclamp(li.y, 0.0f, 1.0f), gclamp(li.z, 0.0f, 1.0f), occ};
 }
 
 // Thread = 2 x 2 pixels (columns 2k, 2k + 1 share pu; rows share pv when W <= H, else
 // the shared terms are computed per row).
-__global__ void __launch_bounds__(256, 5) se_composite_kernel(const MipChain m, const float4* __restrict__ light,
-                                                           const float4* __restrict__ bg, int bw, int bh, float ws0,
-                                                           float ws1, float ws2, float4* __restrict__ out) {
-  const int W = m.w[0], H = m.h[0];
+// d = 1 / pixelate with pixelate = W / 2, as the fragment computes them (host-side, binary32).
+__global__ void __launch_bounds__(256, 5) se_composite_kernel(const CompositeSrc m, const float4* __restrict__ light,
+                                                           const float4* __restrict__ bg, int bw, int bh, float d,
+                                                           float ws0, float ws1, float ws2,
+                                                           float4* __restrict__ out) {
+  const int W = m.w, H = m.h;
   const int c0 = 2 * (blockIdx.x * 32 + (threadIdx.x & 31)), r0 = 2 * (blockIdx.y * 8 + (threadIdx.x >> 5));
   if (c0 >= W || r0 >= H) return;
-  const float pixelate = __fdiv_rn((float)W, 2.0f);
-  const float d = __fdiv_rn(1.0f, pixelate);
   const float u0 = __fdiv_rn(fadd((float)c0, 0.5f), (float)W);
   const float pu = fmul(floorf(__fdiv_rn(u0, d)), d);  // the same for column c0 + 1
   Shared sh[2];
@@ -328,7 +404,7 @@ __global__ void __launch_bounds__(256, 5) se_composite_kernel(const MipChain m, 
       const int cx = c0 + dc;
       if (cx >= W) break;
       const float u = __fdiv_rn(fadd((float)cx, 0.5f), (float)W);
-      float4 col = sample_nearest(m.level[0], W, H, u, v);  // texture(color_tex, uv, 0.0): magnification
+      float4 col = sample_nearest(m.color, W, H, u, v);  // texture(color_tex, uv, 0.0): magnification
       col.x = gclamp(fmul(col.x, shade), 0.0f, 1.0f);
       col.y = gclamp(fmul(col.y, shade), 0.0f, 1.0f);
       col.z = gclamp(fmul(col.z, shade), 0.0f, 1.0f);
@@ -346,17 +422,27 @@ __global__ void __launch_bounds__(256, 5) se_composite_kernel(const MipChain m, 
 
 }  // namespace
 
-cudaError_t render_mip(const float4* src, int sw, int sh, float4* dst, cudaStream_t s) {
+cudaError_t render_mip_alpha(const float* src, int sw, int sh, float* dst, cudaStream_t s) {
   const int dw = mip_next(sw), dh = mip_next(sh);
   dim3 grid((unsigned)((dw + 31) / 32), (unsigned)((dh + 7) / 8));
-  se_mip_kernel<<<grid, 256, 0, s>>>(src, sw, sh, dst, dw, dh);
+  se_mip_alpha_kernel<<<grid, 256, 0, s>>>(src, sw, sh, dst, dw, dh);
   return cudaGetLastError();
 }
 
-cudaError_t render_composite(const MipChain& mips, const float4* light, const float4* bg, int bw, int bh,
+cudaError_t render_color_mip(const uint32_t* grid, const float* noise, float4* out, float* alpha1, int W, int H,
+                             const RenderMat* mats, int nmat, cudaStream_t s) {
+  const int tx = (W + 1) / 2, ty = (H + 1) / 2;
+  dim3 g((unsigned)((tx + 31) / 32), (unsigned)((ty + 7) / 8));
+  se_color_mip_kernel<<<g, 256, 0, s>>>(grid, noise, out, alpha1, W, H, mip_next(W), mip_next(H), mats, nmat);
+  return cudaGetLastError();
+}
+
+cudaError_t render_composite(const CompositeSrc& src, const float4* light, const float4* bg, int bw, int bh,
                              const float w_side[3], float4* out, cudaStream_t s) {
-  dim3 grid((unsigned)((mips.w[0] + 63) / 64), (unsigned)((mips.h[0] + 15) / 16));
-  se_composite_kernel<<<grid, 256, 0, s>>>(mips, light, bg, bw, bh, w_side[0], w_side[1], w_side[2], out);
+  const float pixelate = (float)src.w / 2.0f;  // fragment140.glsl: pixelate = resolution.x / 2
+  const float d = 1.0f / pixelate;
+  dim3 grid((unsigned)((src.w + 63) / 64), (unsigned)((src.h + 15) / 16));
+  se_composite_kernel<<<grid, 256, 0, s>>>(src, light, bg, bw, bh, d, w_side[0], w_side[1], w_side[2], out);
   return cudaGetLastError();
 }
 

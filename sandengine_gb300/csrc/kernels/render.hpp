@@ -35,18 +35,34 @@ cudaError_t light_pass(const uint32_t* old_grid, const uint32_t* new_grid, const
 // pyramid, then one RGBA32F pixel per texel.  GL filtering is fixed to the spec's formulas
 // in binary32 (mirrored-repeat wrap, nearest / bilinear taps, LINEAR_MIPMAP_NEAREST level
 // choice); the three blur weights exp(-gamma) for gamma 0.5, 0.35, 0.2 are passed in.
+// The fragment reads levels above 0 only through their alpha (the occlusion's
+// textureLod(...).a), so those levels are kept as alpha alone: the same box-filter sums of
+// the alpha channel, a quarter of the bytes.
 constexpr int kMaxMipLevels = 24;
-struct MipChain {
-  const float4* level[kMaxMipLevels];
-  int w[kMaxMipLevels], h[kMaxMipLevels];
-  int n;
+// The occlusion's textureLod calls use the integer lods 0 .. 6.
+constexpr int kOccLods = 7;
+// What the composite samples: the colour field (level 0) and, for lod l = 1 .. 6, the alpha
+// level textureLod reads at lod l.  With LINEAR_MIPMAP_NEAREST that is level
+// ceil(l + 0.5) - 1 = l, or the last level of a shorter pyramid; a 1 x 1 field has no level
+// 1, and its slots hold a copy of its own alpha.
+struct CompositeSrc {
+  const float4* color;
+  int w, h;
+  const float* alpha[kOccLods];  // [0] is unused
+  int aw[kOccLods], ah[kOccLods];
 };
 // exp(-gamma) for the three sampleBlurred calls (gamma 0.5, 0.35, 0.2), rounded to binary32.
 constexpr float kBlurSideWeight[3] = {0.606530666f, 0.704688072f, 0.818730772f};
 // Size of the next level: halved, at least 1.
 inline int mip_next(int n) { return n > 1 ? n / 2 : 1; }
-cudaError_t render_mip(const float4* src, int sw, int sh, float4* dst, cudaStream_t s);
-cudaError_t render_composite(const MipChain& mips, const float4* light, const float4* bg, int bw, int bh,
+// output_color as render_color, plus (alpha1 != null) the pyramid's level-1 alpha,
+// mip_next(W) x mip_next(H): a cell's alpha is its material's colour alpha, so the level
+// comes from the same pass instead of a second read of the RGBA field.
+cudaError_t render_color_mip(const uint32_t* grid, const float* noise, float4* out, float* alpha1, int W, int H,
+                             const RenderMat* mats, int nmat, cudaStream_t s);
+// The next alpha level (mip_next(sw) x mip_next(sh)) from an alpha level.
+cudaError_t render_mip_alpha(const float* src, int sw, int sh, float* dst, cudaStream_t s);
+cudaError_t render_composite(const CompositeSrc& src, const float4* light, const float4* bg, int bw, int bh,
                              const float w_side[3], float4* out, cudaStream_t s);
 
 }  // namespace se::rt

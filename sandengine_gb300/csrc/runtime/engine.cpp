@@ -427,7 +427,7 @@ Status World::light_frame() {
   return Status::Ok();
 }
 
-Status World::render_color() {
+Status World::render_color(float* alpha1) {
   TraceRange trace("se_world_render_color");
   if (halo >= 0) return {SE_ERR_INVALID_ARGUMENT, "colours are rendered for whole worlds"};
   if (!d_noise) {
@@ -444,7 +444,10 @@ Status World::render_color() {
     Status s = timing_begin(2, (long long)W * H, 1, &t);
     if (!s.ok()) return s;
   }
-  SE_CUDA(se::rt::render_color(buf[cur], d_noise, d_color, W, H, rs->d_render, rs->num_materials(), stream));
+  if (alpha1)
+    SE_CUDA(render_color_mip(buf[cur], d_noise, d_color, alpha1, W, H, rs->d_render, rs->num_materials(), stream));
+  else
+    SE_CUDA(se::rt::render_color(buf[cur], d_noise, d_color, W, H, rs->d_render, rs->num_materials(), stream));
   if (t) SE_CUDA(cudaEventRecord(t->b, stream));
   return Status::Ok();
 }
@@ -452,28 +455,36 @@ Status World::render_color() {
 Status World::composite(const float* bg, int bw, int bh) {
   TraceRange trace("se_world_composite");
   if (bg && (bw <= 0 || bh <= 0)) return {SE_ERR_INVALID_ARGUMENT, "background size must be positive"};
-  Status s = render_color();
+  // pyramid sizes (level 0 is the colour field); the alpha levels are allocated once, and a
+  // 1 x 1 field keeps a copy of its alpha in place of level 1
+  int lw[kMaxMipLevels], lh[kMaxMipLevels], n = 1;
+  lw[0] = W;
+  lh[0] = H;
+  for (; (lw[n - 1] > 1 || lh[n - 1] > 1) && n < kMaxMipLevels; ++n) {
+    lw[n] = mip_next(lw[n - 1]);
+    lh[n] = mip_next(lh[n - 1]);
+  }
+  for (int l = (int)mips.size() + 1; l < std::max(n, 2); ++l) {
+    float* m = nullptr;
+    cudaError_t e = cudaMalloc(&m, (size_t)(l < n ? lw[l] * lh[l] : 1) * sizeof(float));
+    if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    mips.push_back(m);
+  }
+  // colours and level 1 in one pass, then the smaller levels
+  Status s = render_color(n > 1 ? mips[0] : nullptr);
   if (!s.ok()) return s;
-  MipChain chain{};
-  chain.level[0] = d_color;
-  chain.w[0] = W;
-  chain.h[0] = H;
-  chain.n = 1;
-  for (int w = W, h = H; (w > 1 || h > 1) && chain.n < kMaxMipLevels; ++chain.n) {
-    const int nw = mip_next(w), nh = mip_next(h);
-    if ((int)mips.size() < chain.n) {
-      float4* m = nullptr;
-      cudaError_t e = cudaMalloc(&m, (size_t)nw * nh * sizeof(float4));
-      if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
-      mips.push_back(m);
-    }
-    float4* dst = mips[(size_t)chain.n - 1];
-    SE_CUDA(render_mip(chain.level[chain.n - 1], w, h, dst, stream));
-    chain.level[chain.n] = dst;
-    chain.w[chain.n] = nw;
-    chain.h[chain.n] = nh;
-    w = nw;
-    h = nh;
+  for (int l = 2; l < n; ++l) SE_CUDA(render_mip_alpha(mips[(size_t)l - 2], lw[l - 1], lh[l - 1], mips[(size_t)l - 1], stream));
+  if (n == 1)
+    SE_CUDA(cudaMemcpyAsync(mips[0], &d_color->w, sizeof(float), cudaMemcpyDeviceToDevice, stream));
+  CompositeSrc src{};
+  src.color = d_color;
+  src.w = W;
+  src.h = H;
+  for (int l = 1; l < kOccLods; ++l) {
+    const int lv = std::max(1, std::min(l, n - 1));  // the level textureLod reads at lod l
+    src.alpha[l] = mips[(size_t)lv - 1];
+    src.aw[l] = lv < n ? lw[lv] : 1;
+    src.ah[l] = lv < n ? lh[lv] : 1;
   }
   const float4* bgd = nullptr;
   if (bg) {
@@ -498,7 +509,7 @@ Status World::composite(const float* bg, int bw, int bh) {
     s = timing_begin(3, (long long)W * H, 1, &t);
     if (!s.ok()) return s;
   }
-  SE_CUDA(render_composite(chain, light[0] ? light[lcur] : nullptr, bgd, bw, bh, kBlurSideWeight, d_composite,
+  SE_CUDA(render_composite(src, light[0] ? light[lcur] : nullptr, bgd, bw, bh, kBlurSideWeight, d_composite,
                            stream));
   if (t) SE_CUDA(cudaEventRecord(t->b, stream));
   return Status::Ok();

@@ -115,10 +115,11 @@ struct World {
   float4* d_color = nullptr;
   Status set_light(bool on);
   Status light_frame();  // light pass for the frame just taken (old grid buf[cur ^ 1])
-  Status render_color();  // the current grid's colours into d_color
+  // The current grid's colours into d_color; with alpha1, also the pyramid's level-1 alpha.
+  Status render_color(float* alpha1 = nullptr);
   // Headless composite of the current grid (colour, its pyramid, the light field when
   // kept, an optional background image) into d_composite (RGBA32F per cell).
-  std::vector<float4*> mips;  // colour pyramid levels 1..
+  std::vector<float*> mips;  // the colour pyramid's levels 1.. (alpha only)
   float4* d_composite = nullptr;
   float4* d_bg = nullptr;
   size_t bg_cap = 0;

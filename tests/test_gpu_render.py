@@ -92,11 +92,12 @@ def test_color_matches_port_within_sin_tolerance(se, rulesets, ports, name):
     assert np.array_equal(sim.output_color, got)
 
 
-@pytest.mark.parametrize("shape", [(640, 400), (333, 517), (64, 64)])
+@pytest.mark.parametrize("shape", [(640, 400), (333, 517), (64, 64), (7, 5), (1, 33), (35, 2), (2, 1)])
 def test_composite_matches_port(se, rulesets, ports, shape):
     """The headless composite (fragment140.glsl) equals the oracle's restatement bit for bit
     when both start from the same colour and light fields (the GPU's own), with and
-    without a background image, on non-square and odd-sized worlds."""
+    without a background image, on non-square, odd-sized and one- or two-texel-wide worlds
+    (where the pyramid's box filter clamps its second row or column)."""
     W, H = shape
     P = ports["twelve_materials"]
     rs = se.parse_string(rulesets["twelve_materials"])
