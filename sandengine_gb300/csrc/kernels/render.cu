@@ -275,9 +275,6 @@ __device__ __forceinline__ int mirror_index(int i, int n) {  // GL_MIRRORED_REPE
 __device__ __forceinline__ float4 tap(const float4* t, int w, int h, int i, int j) {
   return __ldg(t + (size_t)mirror_index(j, h) * w + mirror_index(i, w));
 }
-__device__ __forceinline__ float4 sample_nearest(const float4* t, int w, int h, float u, float v) {
-  return tap(t, w, h, (int)floorf(fmul(u, (float)w)), (int)floorf(fmul(v, (float)h)));
-}
 __device__ __forceinline__ float lerp4(float t00, float t10, float t01, float t11, float w00, float w10, float w01,
                                        float w11) {
   return fadd(fadd(fadd(fmul(t00, w00), fmul(t10, w10)), fmul(t01, w01)), fmul(t11, w11));
@@ -369,24 +366,50 @@ __device__ Shared shared_terms(const CompositeSrc& m, const float4* __restrict__
 
 // Thread = 2 x 2 pixels (columns 2k, 2k + 1 share pu; rows share pv when W <= H, else
 // the shared terms are computed per row).
-// d = 1 / pixelate with pixelate = W / 2, as the fragment computes them (host-side, binary32).
-__global__ void __launch_bounds__(256, 5) se_composite_kernel(const CompositeSrc m, const float4* __restrict__ light,
-                                                           const float4* __restrict__ bg, int bw, int bh, float d,
-                                                           float ws0, float ws1, float ws2,
-                                                           float4* __restrict__ out) {
+__device__ __forceinline__ int coords_len(int n) { return (n + 4) & ~3; }  // round_up(n + 1, 4)
+
+// The column and row tables (uv, pixelated uv, nearest texel): one thread per column / row.
+// d = 1 / pixelate with pixelate = W / 2, as the fragment computes them.
+__global__ void __launch_bounds__(256) se_composite_coords_kernel(float* __restrict__ u, int* __restrict__ ix,
+                                                                  float* __restrict__ pu, float* __restrict__ v,
+                                                                  int* __restrict__ iy, float* __restrict__ pv,
+                                                                  int W, int H, float d) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < coords_len(W)) {
+    const float ut = __fdiv_rn(fadd((float)t, 0.5f), (float)W);
+    u[t] = t < W ? ut : 0.0f;
+    ix[t] = t < W ? mirror_index((int)floorf(fmul(ut, (float)W)), W) : 0;
+    // column pair t: its even column 2t (column 2t + 1 pixelates to the same u)
+    const float ue = __fdiv_rn(fadd((float)(2 * t), 0.5f), (float)W);
+    pu[t] = 2 * t < W ? fmul(floorf(__fdiv_rn(ue, d)), d) : 0.0f;
+  }
+  if (t < coords_len(H)) {
+    const float vt = __fdiv_rn(fadd((float)t, 0.5f), (float)H);
+    v[t] = t < H ? vt : 0.0f;
+    iy[t] = t < H ? mirror_index((int)floorf(fmul(vt, (float)H)), H) : 0;
+    pv[t] = t < H ? fmul(floorf(__fdiv_rn(vt, d)), d) : 0.0f;
+  }
+}
+
+__global__ void __launch_bounds__(256, 4) se_composite_kernel(const CompositeSrc m, const CompositeCoords cc,
+                                                           const float4* __restrict__ light,
+                                                           const float4* __restrict__ bg, int bw, int bh, float ws0,
+                                                           float ws1, float ws2, float4* __restrict__ out) {
   const int W = m.w, H = m.h;
   const int c0 = 2 * (blockIdx.x * 32 + (threadIdx.x & 31)), r0 = 2 * (blockIdx.y * 8 + (threadIdx.x >> 5));
   if (c0 >= W || r0 >= H) return;
-  const float u0 = __fdiv_rn(fadd((float)c0, 0.5f), (float)W);
-  const float pu = fmul(floorf(__fdiv_rn(u0, d)), d);  // the same for column c0 + 1
+  // c0 and r0 are even: 8-byte aligned pair loads, in bounds up to index W / H
+  const float2 us = __ldg(reinterpret_cast<const float2*>(cc.u + c0));
+  const int2 ixs = __ldg(reinterpret_cast<const int2*>(cc.ix + c0));
+  const float pu = __ldg(cc.pu + (c0 >> 1));
+  const float2 vs = __ldg(reinterpret_cast<const float2*>(cc.v + r0));
+  const int2 iys = __ldg(reinterpret_cast<const int2*>(cc.iy + r0));
+  const float2 pv2 = __ldg(reinterpret_cast<const float2*>(cc.pv + r0));
+  const float pvs[2] = {pv2.x, pv2.y};
   Shared sh[2];
-  float pvs[2];
 #pragma unroll
   for (int dr = 0; dr < 2; ++dr) {
-    const int r = r0 + dr;
-    if (r >= H) break;
-    const float v = __fdiv_rn(fadd((float)r, 0.5f), (float)H);
-    pvs[dr] = fmul(floorf(__fdiv_rn(v, d)), d);
+    if (r0 + dr >= H) break;
     sh[dr] = (dr == 1 && pvs[1] == pvs[0]) ? sh[0] : shared_terms(m, light, pu, pvs[dr], ws0, ws1, ws2);
   }
   const float ambient = 0.1f;
@@ -394,7 +417,8 @@ __global__ void __launch_bounds__(256, 5) se_composite_kernel(const CompositeSrc
   for (int dr = 0; dr < 2; ++dr) {
     const int r = r0 + dr;
     if (r >= H) break;
-    const float v = __fdiv_rn(fadd((float)r, 0.5f), (float)H);
+    const float v = dr ? vs.y : vs.x;
+    const int ty = dr ? iys.y : iys.x;
     const Shared& S = sh[dr];
     const float sky = fmul(0.5f, fsub(1.0f, pvs[dr]));
     const float shade = fadd(ambient, fmul(S.occ, fsub(1.0f, ambient)));
@@ -403,8 +427,9 @@ __global__ void __launch_bounds__(256, 5) se_composite_kernel(const CompositeSrc
     for (int dc = 0; dc < 2; ++dc) {
       const int cx = c0 + dc;
       if (cx >= W) break;
-      const float u = __fdiv_rn(fadd((float)cx, 0.5f), (float)W);
-      float4 col = sample_nearest(m.color, W, H, u, v);  // texture(color_tex, uv, 0.0): magnification
+      const float u = dc ? us.y : us.x;
+      // texture(color_tex, uv, 0.0): a magnification, the nearest texel
+      float4 col = __ldg(m.color + (size_t)ty * W + (dc ? ixs.y : ixs.x));
       col.x = gclamp(fmul(col.x, shade), 0.0f, 1.0f);
       col.y = gclamp(fmul(col.y, shade), 0.0f, 1.0f);
       col.z = gclamp(fmul(col.z, shade), 0.0f, 1.0f);
@@ -437,12 +462,31 @@ cudaError_t render_color_mip(const uint32_t* grid, const float* noise, float4* o
   return cudaGetLastError();
 }
 
-cudaError_t render_composite(const CompositeSrc& src, const float4* light, const float4* bg, int bw, int bh,
-                             const float w_side[3], float4* out, cudaStream_t s) {
-  const float pixelate = (float)src.w / 2.0f;  // fragment140.glsl: pixelate = resolution.x / 2
+size_t composite_coords_bytes(int W, int H) {
+  return sizeof(float) * 3 * ((size_t)((W + 4) & ~3) + (size_t)((H + 4) & ~3));
+}
+
+cudaError_t render_composite_coords(void* buf, int W, int H, CompositeCoords* out, cudaStream_t s) {
+  const int LW = (W + 4) & ~3, LH = (H + 4) & ~3;
+  float* f = static_cast<float*>(buf);
+  float* u = f;
+  int* ix = reinterpret_cast<int*>(f + LW);
+  float* pu = f + 2 * (size_t)LW;
+  float* v = f + 3 * (size_t)LW;
+  int* iy = reinterpret_cast<int*>(v + LH);
+  float* pv = v + 2 * (size_t)LH;
+  const float pixelate = (float)W / 2.0f;  // fragment140.glsl: pixelate = resolution.x / 2
   const float d = 1.0f / pixelate;
+  const int n = std::max(LW, LH);
+  se_composite_coords_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(u, ix, pu, v, iy, pv, W, H, d);
+  *out = CompositeCoords{u, ix, pu, v, iy, pv};
+  return cudaGetLastError();
+}
+
+cudaError_t render_composite(const CompositeSrc& src, const CompositeCoords& coords, const float4* light,
+                             const float4* bg, int bw, int bh, const float w_side[3], float4* out, cudaStream_t s) {
   dim3 grid((unsigned)((src.w + 63) / 64), (unsigned)((src.h + 15) / 16));
-  se_composite_kernel<<<grid, 256, 0, s>>>(src, light, bg, bw, bh, d, w_side[0], w_side[1], w_side[2], out);
+  se_composite_kernel<<<grid, 256, 0, s>>>(src, coords, light, bg, bw, bh, w_side[0], w_side[1], w_side[2], out);
   return cudaGetLastError();
 }
 

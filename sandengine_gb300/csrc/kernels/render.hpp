@@ -62,7 +62,23 @@ cudaError_t render_color_mip(const uint32_t* grid, const float* noise, float4* o
                              const RenderMat* mats, int nmat, cudaStream_t s);
 // The next alpha level (mip_next(sw) x mip_next(sh)) from an alpha level.
 cudaError_t render_mip_alpha(const float* src, int sw, int sh, float* dst, cudaStream_t s);
-cudaError_t render_composite(const CompositeSrc& src, const float4* light, const float4* bg, int bw, int bh,
-                             const float w_side[3], float4* out, cudaStream_t s);
+// Column and row tables of the composite, functions of the field's size only (built once):
+// u = (c + 0.5) / W and the column of its nearest texel, the pixelated u of each column
+// pair (floor(u / d) * d at its even column, d = 1 / (W / 2)), and per row v, its nearest
+// row and the pixelated v.  Arrays hold round_up(W + 1, 4) / round_up(H + 1, 4) entries, so
+// that the pair loads of an odd last column or row stay in bounds.
+struct CompositeCoords {
+  const float* u;
+  const int* ix;
+  const float* pu;
+  const float* v;
+  const int* iy;
+  const float* pv;
+};
+size_t composite_coords_bytes(int W, int H);
+// Fills `buf` (composite_coords_bytes(W, H), 16-byte aligned) and points `out` into it.
+cudaError_t render_composite_coords(void* buf, int W, int H, CompositeCoords* out, cudaStream_t s);
+cudaError_t render_composite(const CompositeSrc& src, const CompositeCoords& coords, const float4* light,
+                             const float4* bg, int bw, int bh, const float w_side[3], float4* out, cudaStream_t s);
 
 }  // namespace se::rt

@@ -107,6 +107,7 @@ World::~World() {
   if (d_noise) cudaFree(d_noise);
   if (d_color) cudaFree(d_color);
   for (auto* m : mips) cudaFree(m);
+  if (d_coords) cudaFree(d_coords);
   if (copy_stream) cudaStreamSynchronize(copy_stream);
   for (int i = 0; i < 2; ++i) {
     if (stage[i]) cudaFree(stage[i]);
@@ -504,12 +505,17 @@ Status World::composite(const float* bg, int bw, int bh) {
     cudaError_t e = cudaMalloc(&d_composite, (size_t)W * H * sizeof(float4));
     if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
   }
+  if (!d_coords) {
+    cudaError_t e = cudaMalloc(&d_coords, composite_coords_bytes(W, H));
+    if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    SE_CUDA(render_composite_coords(d_coords, W, H, &coords, stream));
+  }
   Timed* t = nullptr;
   if (timing) {
     s = timing_begin(3, (long long)W * H, 1, &t);
     if (!s.ok()) return s;
   }
-  SE_CUDA(render_composite(src, light[0] ? light[lcur] : nullptr, bgd, bw, bh, kBlurSideWeight, d_composite,
+  SE_CUDA(render_composite(src, coords, light[0] ? light[lcur] : nullptr, bgd, bw, bh, kBlurSideWeight, d_composite,
                            stream));
   if (t) SE_CUDA(cudaEventRecord(t->b, stream));
   return Status::Ok();

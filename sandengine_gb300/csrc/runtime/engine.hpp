@@ -120,6 +120,8 @@ struct World {
   // Headless composite of the current grid (colour, its pyramid, the light field when
   // kept, an optional background image) into d_composite (RGBA32F per cell).
   std::vector<float*> mips;  // the colour pyramid's levels 1.. (alpha only)
+  void* d_coords = nullptr;  // the composite's column and row tables (built once)
+  CompositeCoords coords{};
   float4* d_composite = nullptr;
   float4* d_bg = nullptr;
   size_t bg_cap = 0;
