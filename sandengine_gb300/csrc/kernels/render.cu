@@ -149,10 +149,18 @@ __global__ void __launch_bounds__(256) se_color_mip_kernel(const uint32_t* __res
 // cells of a row, so shared-memory reads and global loads / stores are contiguous.
 constexpr int LTW = 64, LTH = 16, LSW = LTW + 2, LSH = LTH + 2;
 
+// GLSL max (a < b ? b : a).  CLEAN: neither argument is NaN or -0, where the hardware
+// maximum returns the same value in one instruction instead of a compare and a select.
+template <bool CLEAN>
+__device__ __forceinline__ float lmax(float a, float b) {
+  return CLEAN ? fmaxf(a, b) : gmax(a, b);
+}
+
 // The 8-neighbour blend for the staged cell s0.  INTERIOR: all 8 neighbours lie in the
 // world (no checks; the mean's division by 8 is the product by 0.125, the same correctly
-// rounded quotient).
-template <bool INTERIOR>
+// rounded quotient).  CLEAN: every staged value is a non-negative number or +inf (so are
+// the running maxima, which start at +0).
+template <bool INTERIOR, bool CLEAN>
 __device__ __forceinline__ float4 light_blend(const float4* sl, const uint8_t* sk, int s0) {
   // neighbours in getDiagonalNeighbours order: DOWN, UP, DOWNLEFT, UPLEFT, DOWNRIGHT,
   // UPRIGHT, RIGHT, LEFT (offsets in the staged array)
@@ -170,11 +178,11 @@ __device__ __forceinline__ float4 light_blend(const float4* sl, const uint8_t* s
     a1 = fadd(a1, t1);
     a2 = fadd(a2, t2);
     a3 = fadd(a3, falloff);
-    maxf = gmax(falloff, maxf);
+    maxf = lmax<CLEAN>(falloff, maxf);
     ++num;
-    m0 = gmax(m0, t0);  // the alpha of the maximum is not used (mix takes .rgb)
-    m1 = gmax(m1, t1);
-    m2 = gmax(m2, t2);
+    m0 = lmax<CLEAN>(m0, t0);  // the alpha of the maximum is not used (mix takes .rgb)
+    m1 = lmax<CLEAN>(m1, t1);
+    m2 = lmax<CLEAN>(m2, t2);
   }
   if (INTERIOR) {
     a0 = fmul(a0, 0.125f);
@@ -193,7 +201,7 @@ __device__ __forceinline__ float4 light_blend(const float4* sl, const uint8_t* s
                      fadd(fmul(a2, 0.5f), fmul(m2, 0.5f)), a3);
 }
 
-__global__ void __launch_bounds__(256, 6) se_light_kernel(const uint32_t* __restrict__ old_grid,
+__global__ void __launch_bounds__(256, 5) se_light_kernel(const uint32_t* __restrict__ old_grid,
                                                        const uint32_t* __restrict__ new_grid,
                                                        const float4* __restrict__ lin, float4* __restrict__ lout,
                                                        int W, int H, const RenderMat* __restrict__ mats, int nmat) {
@@ -225,6 +233,7 @@ __global__ void __launch_bounds__(256, 6) se_light_kernel(const uint32_t* __rest
     const int x = X0 + cx, y = Y0 + (threadIdx.x >> 6) + 4 * j;
     nid[j] = (x < W && y < H) ? __ldg(new_grid + (size_t)y * W + x) : 0u;
   }
+  uint32_t top = 0;  // the largest bit pattern staged by this thread
 #pragma unroll
   for (int u = 0; u < NU; ++u) {
     const int i = threadIdx.x + u * NT;
@@ -233,14 +242,19 @@ __global__ void __launch_bounds__(256, 6) se_light_kernel(const uint32_t* __rest
       const float keep = (__ldg(&mats[mat_index(ids[u], nmat)].flags) & kRenderObstacle) ? 0.0f : 1.0f;
       const float4 l = ls[u];
       // light_data = light * vec4(vec3(keep), 1.0); contribution = (light_data.rgb * a, a)
-      sl[i] = make_float4(fmul(fmul(l.x, keep), l.w), fmul(fmul(l.y, keep), l.w), fmul(fmul(l.z, keep), l.w), l.w);
+      const float4 c =
+          make_float4(fmul(fmul(l.x, keep), l.w), fmul(fmul(l.y, keep), l.w), fmul(fmul(l.z, keep), l.w), l.w);
+      sl[i] = c;
       sk[i] = 0;
+      top = max(top, max(max(__float_as_uint(c.x), __float_as_uint(c.y)),
+                         max(__float_as_uint(c.z), __float_as_uint(c.w))));
     } else {
       sl[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       sk[i] = 1;
     }
   }
-  __syncthreads();
+  // Patterns up to 0x7f800000 are +0 .. +inf: no NaN, no -0 (nor any negative value).
+  const bool clean = !__syncthreads_or(top > 0x7f800000u);
   const bool interior = X0 >= 1 && Y0 >= 1 && X0 + LTW + 1 <= W && Y0 + LTH + 1 <= H;
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -256,7 +270,10 @@ __global__ void __launch_bounds__(256, 6) se_light_kernel(const uint32_t* __rest
       L = make_float4(1.0f, 1.0f, 1.0f, 0.999999f);
     } else {
       const int s0 = (cy + 1) * LSW + cx + 1;
-      L = interior ? light_blend<true>(sl, sk, s0) : light_blend<false>(sl, sk, s0);
+      if (clean)
+        L = interior ? light_blend<true, true>(sl, sk, s0) : light_blend<false, true>(sl, sk, s0);
+      else
+        L = interior ? light_blend<true, false>(sl, sk, s0) : light_blend<false, false>(sl, sk, s0);
     }
     lout[(size_t)y * W + x] = L;
   }

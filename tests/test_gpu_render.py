@@ -55,6 +55,40 @@ def test_light_matches_port_every_frame(se, rulesets, ports, name, shape, frame0
     assert np.count_nonzero(light[..., 3]) > 0
 
 
+def test_light_exact_max_with_nan_and_negative_zero(se, rulesets, ports):
+    """A light field set by the caller may hold -0, NaN, negative or infinite values.  Tiles
+    that stage any of them take GLSL max as written (a compare and a select), the others
+    the hardware maximum; either way the field equals the oracle's.  NaNs are compared as
+    NaNs (GPU arithmetic returns the canonical NaN, the CPU keeps the payload)."""
+    W, H = 200, 90
+    rs = se.parse_string(rulesets["twelve_materials"])
+    P = ports["twelve_materials"]
+    sim = se.Simulation(rs, (W, H))
+    g = wl.patch_fill(W, H, 4, *wl.twelve_fill_spec(), patch=16)
+    sim.grid = g
+    sim.params.frame = 7
+    sim.set_light(True)
+    L = np.random.default_rng(3).random((H, W, 4)).astype(np.float32)
+    # a few tiles (64 x 16 cells) get one unusual value each
+    L[5, 10, 0] = -0.0
+    L[20, 70, 3] = np.nan
+    L[40, 130, 1] = -0.25
+    L[70, 150, 2] = np.inf
+    L[3, 190, 3] = -0.0
+    sim.output_light = L
+    cur, f, light = g.copy(), 7, L.copy()
+    for _ in range(3):
+        sim.run_frames(1)
+        old = cur.copy()
+        P.step(cur, f + 1)
+        f += 1
+        light = P.light(old, cur, light)
+        got = sim.output_light
+        nan = np.isnan(light)
+        assert nan.any() and np.array_equal(np.isnan(got), nan), f"NaN cells, frame {f}"
+        assert np.array_equal(got.view(np.uint32)[~nan], light.view(np.uint32)[~nan]), f"light, frame {f}"
+
+
 def test_light_field_round_trip_and_off(se, rulesets):
     rs = se.parse_string(rulesets["four_materials"])
     sim = se.Simulation(rs, (40, 30))
