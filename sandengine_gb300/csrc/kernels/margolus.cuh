@@ -302,15 +302,16 @@ __device__ __forceinline__ void se_list_push(bool dyn, uint32_t entry, uint16_t*
   if (dyn && se_check(at < cap, 4u)) list[at] = (uint16_t)entry;
 }
 
+// Block rows ly0 + 2 j, j in [jlo, jlo + nby), are collected (the rows a step still needs).
 template <int SW, int SH, int OX, int NT>
-__device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int gx0, int gy0, int f, int W, int H,
-                                                 const uint16_t* __restrict__ lut, uint32_t umask,
+__device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, int nby, int gx0, int gy0, int f,
+                                                 int W, int H, const uint16_t* __restrict__ lut, uint32_t umask,
                                                  uint16_t* __restrict__ list, int* __restrict__ cnt) {
   static_assert(NT % 32 == 0 || NT == 1, "whole warps");
   static_assert(SW % 8 == 0 && SW * SH <= 65536, "8-byte rows, 16-bit offsets");
   constexpr int NBX = (SW - OX) / 2, NCX = NBX / 4, REM = NBX - 4 * NCX;
   constexpr int CAP = (SW / 8) * (SH / 2);  // list capacity (tile_smem_bytes sizes it)
-  const int nby = (SH - ly0) / 2;
+  ly0 += 2 * jlo;
   const int nc = NCX * nby;
   for (int base = threadIdx.x & ~31; base < nc; base += NT) {  // warp-uniform trip count
     const int ci = base + (threadIdx.x & 31);
@@ -607,11 +608,19 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
     const int f = f0 + s;
     const int ly0 = (se_off_y(f) + gy0) & 1;  // gy0 = Y0 - HY is odd when HY is
     if (!edge) {
+      // Rows the stored interior [HY, HY + TH) still depends on after this step: within
+      // k - 1 - s of it.  A block reads only its own cells, so the blocks meeting those
+      // rows (origin rows HY - k + s .. HY + TH + k - 2 - s) are all that step s must
+      // update; the others hold values that no stored cell reads.
+      const int lymin = HY - k + s, lymax = HY + TH + k - 2 - s;
+      const int jlo = lymin > ly0 ? (lymin - ly0 + 1) >> 1 : 0;
+      const int jend = (SH - ly0) / 2 - 1, jneed = (lymax - ly0) >> 1;
+      const int jhi = jneed < jend ? jneed : jend;
       int* c = cnt + (s & 1);
       if (se_off_x(f) == 0)
-        se_chunk_collect<SW, SH, 0, NT>(sm, ly0, gx0, gy0, f, W, H, lut, umask, list, c);
+        se_chunk_collect<SW, SH, 0, NT>(sm, ly0, jlo, jhi - jlo + 1, gx0, gy0, f, W, H, lut, umask, list, c);
       else
-        se_chunk_collect<SW, SH, 1, NT>(sm, ly0, gx0, gy0, f, W, H, lut, umask, list, c);
+        se_chunk_collect<SW, SH, 1, NT>(sm, ly0, jlo, jhi - jlo + 1, gx0, gy0, f, W, H, lut, umask, list, c);
       __syncthreads();
       const int n = *c;
       if (threadIdx.x == 0) cnt[(s + 1) & 1] = 0;  // last read in step s - 1
