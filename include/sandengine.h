@@ -113,7 +113,8 @@ void se_ruleset_free(se_ruleset* rs);
 /* ---- one world (replaces sandengine-core::simulation::Simulation) --------------------- */
 
 /* Simulation::new (simulation.rs:128-192): an all-EMPTY width x height world with frame
- * counter 0 on the current CUDA device.  Compiles the rule set if needed. */
+ * counter 0 on the current CUDA device.  Compiles the rule set if needed.  Sides up to
+ * 1048576 cells and at most 2^36 cells (SE_ERR_INVALID_ARGUMENT beyond). */
 int se_world_create(se_ruleset* rs, int width, int height, se_world** out);
 void se_world_destroy(se_world* w);
 

@@ -56,8 +56,10 @@ __device__ float simplex(float px, float py) {
   return fadd(0.25f, fmul(0.5f, fadd(fadd(fmul(n0, 70.0f), fmul(n1, 70.0f)), fmul(n2, 70.0f))));
 }
 
-__global__ void __launch_bounds__(256) se_noise_kernel(float* __restrict__ out, int W, int H) {
-  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+// The 2D kernels take their row blocks from by0 + blockIdx.y: a tall world is covered by
+// several launches, as a grid's y extent stops at 65535.
+__global__ void __launch_bounds__(256) se_noise_kernel(float* __restrict__ out, int W, int H, int by0) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = (by0 + blockIdx.y) * 8 + (threadIdx.x >> 5);
   if (x >= W || y >= H) return;
   float px = (float)x, py = (float)y, f = 0.0f;
   for (int o = 1; o < 4; ++o) {  // noise(p, 3 octaves, lacunarity 2, frequency 0.25)
@@ -108,8 +110,8 @@ __device__ __forceinline__ float4 cell_color(uint32_t id, float nz, const Render
 __global__ void __launch_bounds__(256) se_color_mip_kernel(const uint32_t* __restrict__ grid,
                                                            const float* __restrict__ noise, float4* __restrict__ out,
                                                            float* __restrict__ alpha1, int W, int H, int dw, int dh,
-                                                           const RenderMat* __restrict__ mats, int nmat) {
-  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+                                                           const RenderMat* __restrict__ mats, int nmat, int by0) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = (by0 + blockIdx.y) * 8 + (threadIdx.x >> 5);
   const int c0 = 2 * x, r0 = 2 * y;
   if (c0 >= W || r0 >= H) return;
   const bool pair = c0 + 1 < W;
@@ -201,14 +203,19 @@ __device__ __forceinline__ float4 light_blend(const float4* sl, const uint8_t* s
                      fadd(fmul(a2, 0.5f), fmul(m2, 0.5f)), a3);
 }
 
+// TALL: the row blocks start at by0 (a world with more than 65535 of them takes several
+// launches); otherwise by0 is 0 and unused, which keeps the common kernel's code as tight
+// as it measured best.
+template <bool TALL>
 __global__ void __launch_bounds__(256, 5) se_light_kernel(const uint32_t* __restrict__ old_grid,
                                                        const uint32_t* __restrict__ new_grid,
                                                        const float4* __restrict__ lin, float4* __restrict__ lout,
-                                                       int W, int H, const RenderMat* __restrict__ mats, int nmat) {
+                                                       int W, int H, const RenderMat* __restrict__ mats, int nmat,
+                                                       int by0) {
   constexpr int NT = 256, NS = LSW * LSH, NU = (NS + NT - 1) / NT;
   __shared__ float4 sl[NS];  // contribution (rgb * keep * a, a) per staged cell
   __shared__ uint8_t sk[NS];  // 1: outside the world
-  const int X0 = blockIdx.x * LTW, Y0 = blockIdx.y * LTH;
+  const int X0 = blockIdx.x * LTW, Y0 = (TALL ? by0 + (int)blockIdx.y : (int)blockIdx.y) * LTH;
   // Issue every global load of this thread first (staged ids and light, then the new ids
   // of its four cells), so that they are in flight together.
   uint32_t ids[NU];
@@ -350,8 +357,8 @@ __device__ __forceinline__ float blurred_alpha(float lo, float mid, float hi, fl
 }
 
 __global__ void __launch_bounds__(256) se_mip_alpha_kernel(const float* __restrict__ src, int sw, int sh,
-                                                           float* __restrict__ dst, int dw, int dh) {
-  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+                                                           float* __restrict__ dst, int dw, int dh, int by0) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = (by0 + blockIdx.y) * 8 + (threadIdx.x >> 5);
   if (x >= dw || y >= dh) return;
   const int x0 = min(2 * x, sw - 1), x1 = min(2 * x + 1, sw - 1), y0 = min(2 * y, sh - 1), y1 = min(2 * y + 1, sh - 1);
   const float a = __ldg(src + (size_t)y0 * sw + x0), b = __ldg(src + (size_t)y0 * sw + x1),
@@ -411,9 +418,9 @@ __global__ void __launch_bounds__(256) se_composite_coords_kernel(float* __restr
 __global__ void __launch_bounds__(256, 4) se_composite_kernel(const CompositeSrc m, const CompositeCoords cc,
                                                            const float4* __restrict__ light,
                                                            const float4* __restrict__ bg, int bw, int bh, float ws0,
-                                                           float ws1, float ws2, float4* __restrict__ out) {
+                                                           float ws1, float ws2, float4* __restrict__ out, int by0) {
   const int W = m.w, H = m.h;
-  const int c0 = 2 * (blockIdx.x * 32 + (threadIdx.x & 31)), r0 = 2 * (blockIdx.y * 8 + (threadIdx.x >> 5));
+  const int c0 = 2 * (blockIdx.x * 32 + (threadIdx.x & 31)), r0 = 2 * ((by0 + blockIdx.y) * 8 + (threadIdx.x >> 5));
   if (c0 >= W || r0 >= H) return;
   // c0 and r0 are even: 8-byte aligned pair loads, in bounds up to index W / H
   const float2 us = __ldg(reinterpret_cast<const float2*>(cc.u + c0));
@@ -462,20 +469,29 @@ __global__ void __launch_bounds__(256, 4) se_composite_kernel(const CompositeSrc
   }
 }
 
+// Launches fn(by0, n) for the row blocks [by0, by0 + n) of a 2D grid, n <= 65535.
+template <class F>
+void for_row_blocks(int blocks, F&& fn) {
+  for (int by0 = 0; by0 < blocks; by0 += 65535) fn(by0, (unsigned)std::min(65535, blocks - by0));
+}
+
 }  // namespace
 
 cudaError_t render_mip_alpha(const float* src, int sw, int sh, float* dst, cudaStream_t s) {
   const int dw = mip_next(sw), dh = mip_next(sh);
-  dim3 grid((unsigned)((dw + 31) / 32), (unsigned)((dh + 7) / 8));
-  se_mip_alpha_kernel<<<grid, 256, 0, s>>>(src, sw, sh, dst, dw, dh);
+  for_row_blocks((dh + 7) / 8, [&](int by0, unsigned n) {
+    se_mip_alpha_kernel<<<dim3((unsigned)((dw + 31) / 32), n), 256, 0, s>>>(src, sw, sh, dst, dw, dh, by0);
+  });
   return cudaGetLastError();
 }
 
 cudaError_t render_color_mip(const uint32_t* grid, const float* noise, float4* out, float* alpha1, int W, int H,
                              const RenderMat* mats, int nmat, cudaStream_t s) {
   const int tx = (W + 1) / 2, ty = (H + 1) / 2;
-  dim3 g((unsigned)((tx + 31) / 32), (unsigned)((ty + 7) / 8));
-  se_color_mip_kernel<<<g, 256, 0, s>>>(grid, noise, out, alpha1, W, H, mip_next(W), mip_next(H), mats, nmat);
+  for_row_blocks((ty + 7) / 8, [&](int by0, unsigned n) {
+    se_color_mip_kernel<<<dim3((unsigned)((tx + 31) / 32), n), 256, 0, s>>>(grid, noise, out, alpha1, W, H,
+                                                                            mip_next(W), mip_next(H), mats, nmat, by0);
+  });
   return cudaGetLastError();
 }
 
@@ -502,14 +518,17 @@ cudaError_t render_composite_coords(void* buf, int W, int H, CompositeCoords* ou
 
 cudaError_t render_composite(const CompositeSrc& src, const CompositeCoords& coords, const float4* light,
                              const float4* bg, int bw, int bh, const float w_side[3], float4* out, cudaStream_t s) {
-  dim3 grid((unsigned)((src.w + 63) / 64), (unsigned)((src.h + 15) / 16));
-  se_composite_kernel<<<grid, 256, 0, s>>>(src, coords, light, bg, bw, bh, w_side[0], w_side[1], w_side[2], out);
+  for_row_blocks((src.h + 15) / 16, [&](int by0, unsigned n) {
+    se_composite_kernel<<<dim3((unsigned)((src.w + 63) / 64), n), 256, 0, s>>>(src, coords, light, bg, bw, bh, w_side[0],
+                                                                              w_side[1], w_side[2], out, by0);
+  });
   return cudaGetLastError();
 }
 
 cudaError_t render_noise(float* noise, int W, int H, cudaStream_t s) {
-  dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
-  se_noise_kernel<<<grid, 256, 0, s>>>(noise, W, H);
+  for_row_blocks((H + 7) / 8, [&](int by0, unsigned n) {
+    se_noise_kernel<<<dim3((unsigned)((W + 31) / 32), n), 256, 0, s>>>(noise, W, H, by0);
+  });
   return cudaGetLastError();
 }
 
@@ -526,8 +545,15 @@ cudaError_t render_color(const uint32_t* grid, const float* noise, float4* out, 
 
 cudaError_t light_pass(const uint32_t* old_grid, const uint32_t* new_grid, const float4* light_in, float4* light_out,
                        int W, int H, const RenderMat* mats, int nmat, cudaStream_t s) {
-  dim3 grid((unsigned)((W + LTW - 1) / LTW), (unsigned)((H + LTH - 1) / LTH));
-  se_light_kernel<<<grid, 256, 0, s>>>(old_grid, new_grid, light_in, light_out, W, H, mats, nmat);
+  const int rows = (H + LTH - 1) / LTH;
+  const dim3 g((unsigned)((W + LTW - 1) / LTW), (unsigned)std::min(rows, 65535));
+  if (rows <= 65535)
+    se_light_kernel<false><<<g, 256, 0, s>>>(old_grid, new_grid, light_in, light_out, W, H, mats, nmat, 0);
+  else
+    for_row_blocks(rows, [&](int by0, unsigned n) {
+      se_light_kernel<true><<<dim3(g.x, n), 256, 0, s>>>(old_grid, new_grid, light_in, light_out, W, H, mats, nmat,
+                                                         by0);
+    });
   return cudaGetLastError();
 }
 

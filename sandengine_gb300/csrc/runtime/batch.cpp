@@ -50,6 +50,8 @@ Status Batch::create(std::shared_ptr<Ruleset> r, int count, const int* widths, c
   std::vector<size_t> off(2 * (size_t)n);
   for (int i = 0; i < n; ++i) {
     if (widths[i] <= 0 || heights[i] <= 0) return {SE_ERR_INVALID_ARGUMENT, "world sizes must be positive"};
+    if (widths[i] > kMaxSide || heights[i] > kMaxSide)
+      return {SE_ERR_INVALID_ARGUMENT, "world sides are limited to 1048576 cells"};
     const size_t b = ((size_t)widths[i] * heights[i] * 4 + 255) & ~(size_t)255;
     off[2 * i] = bytes;
     bytes += b;

@@ -123,6 +123,7 @@ World::~World() {
 
 Status World::create(std::shared_ptr<Ruleset> r, int w, int h) {
   if (w <= 0 || h <= 0) return {SE_ERR_INVALID_ARGUMENT, "world size must be positive"};
+  if (w > kMaxSide || h > kMaxSide) return {SE_ERR_INVALID_ARGUMENT, "world sides are limited to 1048576 cells"};
   if ((int64_t)w * h > (int64_t)1 << 36) return {SE_ERR_INVALID_ARGUMENT, "world too large"};
   rs = std::move(r);
   W = w;
@@ -149,6 +150,7 @@ Status World::create(std::shared_ptr<Ruleset> r, int w, int h) {
 Status World::create_band(std::shared_ptr<Ruleset> r, int w, int world_h, int row0, int rows, int hal) {
   if (w <= 0 || world_h <= 0 || rows <= 0 || row0 < 0 || (int64_t)row0 + rows > world_h || hal < 0)
     return {SE_ERR_INVALID_ARGUMENT, "band rows must lie within the world and the halo be >= 0"};
+  if (w > kMaxSide || world_h > kMaxSide) return {SE_ERR_INVALID_ARGUMENT, "world sides are limited to 1048576 cells"};
   const int a = std::max(0, row0 - hal), b = (int)std::min<int64_t>(world_h, (int64_t)row0 + rows + hal);
   wh = world_h;
   ya = a;
@@ -467,7 +469,7 @@ Status World::composite(const float* bg, int bw, int bh) {
   }
   for (int l = (int)mips.size() + 1; l < std::max(n, 2); ++l) {
     float* m = nullptr;
-    cudaError_t e = cudaMalloc(&m, (size_t)(l < n ? lw[l] * lh[l] : 1) * sizeof(float));
+    cudaError_t e = cudaMalloc(&m, (l < n ? (size_t)lw[l] * (size_t)lh[l] : 1) * sizeof(float));
     if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
     mips.push_back(m);
   }

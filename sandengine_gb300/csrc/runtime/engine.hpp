@@ -17,6 +17,10 @@ struct se_modification;
 
 namespace se::rt {
 
+// Longest world side (cells): tile grids stay within a launch's 65535 rows of CTAs.  A world
+// also holds at most 2^36 cells.
+constexpr int kMaxSide = 1 << 20;
+
 struct Status {
   int code = 0;
   std::string msg;

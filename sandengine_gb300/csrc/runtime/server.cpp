@@ -103,6 +103,7 @@ void Server::release(size_t off, size_t bytes) {
 
 Status Server::open_session(int w, int h, const uint32_t* cells, int32_t frame, int* id) {
   if (w <= 0 || h <= 0) return {SE_ERR_INVALID_ARGUMENT, "session size must be positive"};
+  if (w > kMaxSide || h > kMaxSide) return {SE_ERR_INVALID_ARGUMENT, "world sides are limited to 1048576 cells"};
   if (frame < 0) return {SE_ERR_INVALID_ARGUMENT, "frame must be >= 0"};
   if (session_bytes(w, h) > budget) return {SE_ERR_BUDGET, "the session alone exceeds the HBM budget"};
   Session s;

@@ -37,6 +37,10 @@ def test_bad_arguments_return_status(se):
     assert L.se_ruleset_text(rs.handle, 0, buf, 8, ctypes.byref(n)) == 13  # buffer too small
     assert n.value > 8
     assert L.se_world_create(rs.handle, 0, 5, ctypes.byref(out)) == 1
+    # sides up to 2^20 cells, at most 2^36 cells: refused before any device work
+    for w, h, msg in [((1 << 20) + 1, 4, b"sides"), (4, (1 << 20) + 1, b"sides"), (1 << 20, 1 << 17, b"too large")]:
+        assert L.se_world_create(rs.handle, w, h, ctypes.byref(out)) == 1
+        assert msg in L.se_last_error()
     assert L.se_version() >= 100
 
 

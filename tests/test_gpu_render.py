@@ -89,6 +89,29 @@ def test_light_exact_max_with_nan_and_negative_zero(se, rulesets, ports):
         assert np.array_equal(got.view(np.uint32)[~nan], light.view(np.uint32)[~nan]), f"light, frame {f}"
 
 
+def test_tall_world_spans_several_launches(se, rulesets, ports):
+    """A world 2^20 rows tall has more row blocks than one launch's grid holds (65535), so
+    the light, colour and composite passes are split over launches; grid, light and
+    composite still equal the oracle bit for bit."""
+    W, H = 8, 1 << 20
+    P = ports["four_materials"]
+    sim = se.Simulation(se.parse_string(rulesets["four_materials"]), (W, H))
+    g = wl.patch_fill(W, H, 5, [0, 3, 4, 5], [0.6, 0.2, 0.15, 0.05], patch=4)
+    sim.grid = g
+    sim.params.frame = 3
+    sim.set_light(True)
+    sim.run_frames(2)
+    cur, light = g.copy(), np.zeros((H, W, 4), dtype=np.float32)
+    for f in (4, 5):
+        old = cur.copy()
+        P.step(cur, f)
+        light = P.light(old, cur, light)
+    assert np.array_equal(sim.grid, cur)
+    assert np.array_equal(sim.output_light.view(np.uint32), light.view(np.uint32))
+    col = sim.output_color
+    assert np.array_equal(sim.composite().view(np.uint32), P.composite(col, light).view(np.uint32))
+
+
 def test_light_field_round_trip_and_off(se, rulesets):
     rs = se.parse_string(rulesets["four_materials"])
     sim = se.Simulation(rs, (40, 30))
