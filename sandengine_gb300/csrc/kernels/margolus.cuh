@@ -170,39 +170,19 @@ __device__ __forceinline__ void se_block_store(uint8_t* p, int SW, uint32_t a, u
   }
 }
 
-// One step over the shared array: every block wholly inside it.  OX and ly0 are the
-// parities of the first block column / row in shared-array coordinates: a block's global
-// top-left cell is congruent to the frame's offset modulo 2, and the array starts at global
-// (gx0, gy0).  OX is compile-time so the block index split is a constant division.
-template <int SW, int SH, int OX, int NT>
-__device__ __forceinline__ void se_tile_step(uint8_t* sm, int ly0, int gx0, int gy0, int f, int W, int H,
-                                             bool edge, const uint16_t* __restrict__ lut) {
-  constexpr int NBX = (SW - OX) / 2;
-  const int nb = NBX * ((SH - ly0) / 2);
-  for (int bi = threadIdx.x; bi < nb; bi += NT) {
-    const int j = bi / NBX, i = bi - j * NBX;
-    const int lx = OX + 2 * i, ly = ly0 + 2 * j;
-    if (!se_check(ly >= 0 && lx >= 0 && (ly + 1) * SW + lx + 1 < SW * SH, 2u)) continue;
-    uint8_t* p = sm + ly * SW + lx;
-    uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
-    if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
-    const int gx = gx0 + lx, gy = gy0 + ly;
-    se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
-    se_block_store(p, SW, a, b, c, d, gx, gy, W, H, edge);
-  }
-}
-
 #ifndef SE_LUT
 #define SE_LUT_SMEM_BYTES 0u
 #endif
-// Interior tiles run each step in two phases over chunks of four horizontally adjacent
+// Every tile runs each step in two phases over chunks of four horizontally adjacent
 // blocks (8 cells x 2 rows):
 //  1. se_chunk_collect reads every chunk with two 8-byte loads.  A chunk whose 16 cells are
 //     one material m whose block of four m cells never changes is left as it is (with a
 //     transition table: EMPTY, and in a typical rule set the solids and liquids at rest;
 //     without one: EMPTY, which the shader itself leaves alone); the others are appended
 //     to a list of array offsets (a warp reserves its slots with one atomicAdd).  The
-//     blocks of a row past its last whole chunk are updated right there.
+//     blocks of a row past its last whole chunk are updated right there, and so are, in a
+//     tile reaching past the world, the chunks with cells outside it (block by block,
+//     those cells kept WALL); chunks wholly outside the world are left alone.
 //  2. se_chunk_process updates the listed chunks, one chunk per thread: with a table
 //     word-wide and with four independent lookups, else block by block with the rules.
 // Chunks are skipped whole, so the lanes that evaluate blocks do so together rather than
@@ -303,7 +283,10 @@ __device__ __forceinline__ void se_list_push(bool dyn, uint32_t entry, uint16_t*
 }
 
 // Block rows ly0 + 2 j, j in [jlo, jlo + nby), are collected (the rows a step still needs).
-template <int SW, int SH, int OX, int NT>
+// In an edge tile (part of the array outside the world) chunks wholly outside the world are
+// left alone, chunks partly outside are updated here block by block with the slots outside
+// the world kept WALL, and only chunks of world cells go to the list.
+template <int SW, int SH, int OX, int NT, bool EDGE>
 __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, int nby, int gx0, int gy0, int f,
                                                  int W, int H, const uint16_t* __restrict__ lut, uint32_t umask,
                                                  uint16_t* __restrict__ list, int* __restrict__ cnt) {
@@ -322,12 +305,28 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, 
       off = (ly0 + 2 * j) * SW + OX + 8 * q;
       // chunk loads at odd offsets read up to 3 bytes past the chunk: the 16-byte slack
       if (!se_check(off >= 0 && off + SW + 11 <= ((SW * SH + 15) & ~15) + 16, 8u)) off = 0;
-      uint32_t a0, a1, b0, b1;
-      se_ld8<OX>(sm + off, a0, a1);
-      se_ld8<OX>(sm + off + SW, b0, b1);
-      const uint32_t m = a0 & 0xffu;
-      const bool uniform = ((a0 ^ a1) | (a0 ^ b0) | (a0 ^ b1)) == 0u && a0 == m * 0x01010101u;
-      dyn = !(uniform && m < 16u && ((umask >> m) & 1u));
+      bool inside = true;
+      if (EDGE) {
+        const int gx = gx0 + OX + 8 * q, gy = gy0 + ly0 + 2 * j;
+        inside = gx >= 0 && gx + 7 < W && gy >= 0 && gy + 1 < H;
+        if (!inside && gx + 7 >= 0 && gx < W && gy + 1 >= 0 && gy < H) {
+          for (int kb = 0; kb < 4; ++kb) {
+            uint8_t* p = sm + off + 2 * kb;
+            uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+            if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
+            se_block_update(a, b, c, d, gx + 2 * kb, gy, f, W, H, lut);
+            se_block_store(p, SW, a, b, c, d, gx + 2 * kb, gy, W, H, true);
+          }
+        }
+      }
+      if (inside) {
+        uint32_t a0, a1, b0, b1;
+        se_ld8<OX>(sm + off, a0, a1);
+        se_ld8<OX>(sm + off + SW, b0, b1);
+        const uint32_t m = a0 & 0xffu;
+        const bool uniform = ((a0 ^ a1) | (a0 ^ b0) | (a0 ^ b1)) == 0u && a0 == m * 0x01010101u;
+        dyn = !(uniform && m < 16u && ((umask >> m) & 1u));
+      }
     }
     se_list_push(dyn, (uint32_t)off, list, cnt, CAP);
   }
@@ -341,7 +340,7 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, 
       if ((a | b | c | d) == 0u) continue;
       const int gx = gx0 + lx, gy = gy0 + ly;
       se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
-      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, false);
+      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, EDGE);
     }
   }
 }
@@ -607,34 +606,34 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   for (int s = 0; s < k; ++s) {
     const int f = f0 + s;
     const int ly0 = (se_off_y(f) + gy0) & 1;  // gy0 = Y0 - HY is odd when HY is
-    if (!edge) {
-      // Rows the stored interior [HY, HY + TH) still depends on after this step: within
-      // k - 1 - s of it.  A block reads only its own cells, so the blocks meeting those
-      // rows (origin rows HY - k + s .. HY + TH + k - 2 - s) are all that step s must
-      // update; the others hold values that no stored cell reads.
-      const int lymin = HY - k + s, lymax = HY + TH + k - 2 - s;
-      const int jlo = lymin > ly0 ? (lymin - ly0 + 1) >> 1 : 0;
-      const int jend = (SH - ly0) / 2 - 1, jneed = (lymax - ly0) >> 1;
-      const int jhi = jneed < jend ? jneed : jend;
-      int* c = cnt + (s & 1);
+    // Rows the stored interior [HY, HY + TH) still depends on after this step: within
+    // k - 1 - s of it.  A block reads only its own cells, so the blocks meeting those
+    // rows (origin rows HY - k + s .. HY + TH + k - 2 - s) are all that step s must
+    // update; the others hold values that no stored cell reads.
+    const int lymin = HY - k + s, lymax = HY + TH + k - 2 - s;
+    const int jlo = lymin > ly0 ? (lymin - ly0 + 1) >> 1 : 0;
+    const int jend = (SH - ly0) / 2 - 1, jneed = (lymax - ly0) >> 1;
+    const int jhi = jneed < jend ? jneed : jend;
+    int* c = cnt + (s & 1);
+    const int nby = jhi - jlo + 1;
+    if (edge) {
       if (se_off_x(f) == 0)
-        se_chunk_collect<SW, SH, 0, NT>(sm, ly0, jlo, jhi - jlo + 1, gx0, gy0, f, W, H, lut, umask, list, c);
+        se_chunk_collect<SW, SH, 0, NT, true>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
       else
-        se_chunk_collect<SW, SH, 1, NT>(sm, ly0, jlo, jhi - jlo + 1, gx0, gy0, f, W, H, lut, umask, list, c);
-      __syncthreads();
-      const int n = *c;
-      if (threadIdx.x == 0) cnt[(s + 1) & 1] = 0;  // last read in step s - 1
+        se_chunk_collect<SW, SH, 1, NT, true>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
+    } else {
       if (se_off_x(f) == 0)
-        se_chunk_process<SW, SH, 0, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
+        se_chunk_collect<SW, SH, 0, NT, false>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
       else
-        se_chunk_process<SW, SH, 1, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
-      __syncthreads();
-      continue;
+        se_chunk_collect<SW, SH, 1, NT, false>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
     }
+    __syncthreads();
+    const int n = *c;
+    if (threadIdx.x == 0) cnt[(s + 1) & 1] = 0;  // last read in step s - 1
     if (se_off_x(f) == 0)
-      se_tile_step<SW, SH, 0, NT>(sm, ly0, gx0, gy0, f, W, H, edge, lut);
+      se_chunk_process<SW, SH, 0, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
     else
-      se_tile_step<SW, SH, 1, NT>(sm, ly0, gx0, gy0, f, W, H, edge, lut);
+      se_chunk_process<SW, SH, 1, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
     __syncthreads();
   }
 
