@@ -189,8 +189,9 @@ __device__ __forceinline__ void se_block_store(uint8_t* p, int SW, uint32_t a, u
 // waiting on one another; blocks of one step are disjoint, so the list order is free.
 
 // Shared-memory layout after the cell array and the table copy: 16 bytes of slack (chunk
-// loads at odd offsets read up to 3 bytes past a row), the two list counters used by
-// alternate steps, one flag byte per material id < 16, then the list.
+// loads at odd offsets read up to 3 bytes past a row), the list counters of alternate steps
+// (chunks to evaluate, then chunks with cells outside the world, which fill the list from
+// its far end), one flag byte per material id < 16, then the list.
 #define SE_HDR_CNT 16
 #define SE_HDR_FLAGS 32
 #define SE_HDR_LIST 48
@@ -269,7 +270,8 @@ __device__ __forceinline__ uint32_t se_lut_fetch(const uint16_t* __restrict__ lu
 #endif
 
 // Appends `entry` for the lanes with `dyn` set; every lane of the warp calls it.  The list
-// holds `cap` entries.
+// holds `cap` entries; DOWN fills it from the far end (entry i at cap - 1 - i).
+template <bool DOWN = false>
 __device__ __forceinline__ void se_list_push(bool dyn, uint32_t entry, uint16_t* __restrict__ list,
                                              int* __restrict__ cnt, int cap) {
   const uint32_t m = __ballot_sync(0xffffffffu, dyn);
@@ -279,17 +281,18 @@ __device__ __forceinline__ void se_list_push(bool dyn, uint32_t entry, uint16_t*
   if (lane == 0) base = atomicAdd(cnt, __popc(m));
   base = __shfl_sync(0xffffffffu, base, 0);
   const int at = base + __popc(m & ((1u << lane) - 1u));
-  if (dyn && se_check(at < cap, 4u)) list[at] = (uint16_t)entry;
+  if (dyn && se_check(at < cap, 4u)) list[DOWN ? cap - 1 - at : at] = (uint16_t)entry;
 }
 
 // Block rows ly0 + 2 j, j in [jlo, jlo + nby), are collected (the rows a step still needs).
 // In an edge tile (part of the array outside the world) chunks wholly outside the world are
-// left alone, chunks partly outside are updated here block by block with the slots outside
-// the world kept WALL, and only chunks of world cells go to the list.
+// left alone, and chunks partly outside go to the far end of the list (counted in bcnt),
+// to be updated block by block with the slots outside the world kept WALL.
 template <int SW, int SH, int OX, int NT, bool EDGE>
 __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, int nby, int gx0, int gy0, int f,
                                                  int W, int H, const uint16_t* __restrict__ lut, uint32_t umask,
-                                                 uint16_t* __restrict__ list, int* __restrict__ cnt) {
+                                                 uint16_t* __restrict__ list, int* __restrict__ cnt,
+                                                 int* __restrict__ bcnt) {
   static_assert(NT % 32 == 0 || NT == 1, "whole warps");
   static_assert(SW % 8 == 0 && SW * SH <= 65536, "8-byte rows, 16-bit offsets");
   constexpr int NBX = (SW - OX) / 2, NCX = NBX / 4, REM = NBX - 4 * NCX;
@@ -298,7 +301,7 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, 
   const int nc = NCX * nby;
   for (int base = threadIdx.x & ~31; base < nc; base += NT) {  // warp-uniform trip count
     const int ci = base + (threadIdx.x & 31);
-    bool dyn = false;
+    bool dyn = false, border = false;
     int off = 0;
     if (ci < nc) {
       const int j = ci / NCX, q = ci - j * NCX;
@@ -309,15 +312,7 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, 
       if (EDGE) {
         const int gx = gx0 + OX + 8 * q, gy = gy0 + ly0 + 2 * j;
         inside = gx >= 0 && gx + 7 < W && gy >= 0 && gy + 1 < H;
-        if (!inside && gx + 7 >= 0 && gx < W && gy + 1 >= 0 && gy < H) {
-          for (int kb = 0; kb < 4; ++kb) {
-            uint8_t* p = sm + off + 2 * kb;
-            uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
-            if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
-            se_block_update(a, b, c, d, gx + 2 * kb, gy, f, W, H, lut);
-            se_block_store(p, SW, a, b, c, d, gx + 2 * kb, gy, W, H, true);
-          }
-        }
+        border = !inside && gx + 7 >= 0 && gx < W && gy + 1 >= 0 && gy < H;
       }
       if (inside) {
         uint32_t a0, a1, b0, b1;
@@ -329,6 +324,7 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, 
       }
     }
     se_list_push(dyn, (uint32_t)off, list, cnt, CAP);
+    if (EDGE) se_list_push<true>(border, (uint32_t)off, list, bcnt, CAP);
   }
   if (REM) {  // blocks past the last whole chunk of each row
     for (int t = threadIdx.x; t < nby * REM; t += NT) {
@@ -384,8 +380,10 @@ __device__ __forceinline__ void se_chunk_eval(uint8_t* p, int SW, uint32_t x, co
 #endif
 
 template <int SW, int SH, int OX, int NT>
-__device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int gx0,
-                                                 int gy0, int f, int W, int H, const uint16_t* __restrict__ lut) {
+__device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int nb,
+                                                 int gx0, int gy0, int f, int W, int H,
+                                                 const uint16_t* __restrict__ lut) {
+  constexpr int CAP = (SW / 8) * (SH / 2);
   const uint32_t xf = (uint32_t)f * 4541161u;
   for (int i = threadIdx.x; i < n; i += NT) {
     if (!se_check(i < (SW / 8) * (SH / 2), 4u)) break;
@@ -408,6 +406,21 @@ __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __
       p[SW + 1] = (uint8_t)d;
     }
 #endif
+  }
+  // chunks with cells outside the world (edge tiles), from the far end of the list
+  for (int i = threadIdx.x; i < nb; i += NT) {
+    if (!se_check(i < CAP, 4u)) break;
+    const int off = list[CAP - 1 - i];
+    if (!se_check(off + SW + 7 < SW * SH, 8u)) continue;
+    const int ly = off / SW, lx = off - ly * SW;
+    for (int kb = 0; kb < 4; ++kb) {
+      uint8_t* p = sm + off + 2 * kb;
+      uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+      if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
+      const int gx = gx0 + lx + 2 * kb, gy = gy0 + ly;
+      se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
+      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, true);
+    }
   }
 }
 
@@ -543,7 +556,7 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   int* cnt = reinterpret_cast<int*>(se_smem + HDR + SE_HDR_CNT);
   uint8_t* flags = se_smem + HDR + SE_HDR_FLAGS;
   uint16_t* list = reinterpret_cast<uint16_t*>(se_smem + HDR + SE_HDR_LIST);
-  for (int i = threadIdx.x; i < 2; i += NT) cnt[i] = 0;
+  for (int i = threadIdx.x; i < 4; i += NT) cnt[i] = 0;  // [s & 1]: to evaluate, [2 + (s & 1)]: border
   se_uniform_flags(lut, flags, NT);
   lut = se_lut_to_smem(lut, se_smem, (SW * SH + 15) & ~15, NT);
   const int gx0 = X0 - HX, gy0 = Y0 - HY;
@@ -615,25 +628,26 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
     const int jend = (SH - ly0) / 2 - 1, jneed = (lymax - ly0) >> 1;
     const int jhi = jneed < jend ? jneed : jend;
     int* c = cnt + (s & 1);
+    int* bc = cnt + 2 + (s & 1);
     const int nby = jhi - jlo + 1;
     if (edge) {
       if (se_off_x(f) == 0)
-        se_chunk_collect<SW, SH, 0, NT, true>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
+        se_chunk_collect<SW, SH, 0, NT, true>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c, bc);
       else
-        se_chunk_collect<SW, SH, 1, NT, true>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
+        se_chunk_collect<SW, SH, 1, NT, true>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c, bc);
     } else {
       if (se_off_x(f) == 0)
-        se_chunk_collect<SW, SH, 0, NT, false>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
+        se_chunk_collect<SW, SH, 0, NT, false>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c, bc);
       else
-        se_chunk_collect<SW, SH, 1, NT, false>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
+        se_chunk_collect<SW, SH, 1, NT, false>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c, bc);
     }
     __syncthreads();
-    const int n = *c;
-    if (threadIdx.x == 0) cnt[(s + 1) & 1] = 0;  // last read in step s - 1
+    const int n = *c, nb = *bc;
+    if (threadIdx.x == 0) cnt[(s + 1) & 1] = cnt[2 + ((s + 1) & 1)] = 0;  // last read in step s - 1
     if (se_off_x(f) == 0)
-      se_chunk_process<SW, SH, 0, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
+      se_chunk_process<SW, SH, 0, NT>(sm, list, n, nb, gx0, gy0, f, W, H, lut);
     else
-      se_chunk_process<SW, SH, 1, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
+      se_chunk_process<SW, SH, 1, NT>(sm, list, n, nb, gx0, gy0, f, W, H, lut);
     __syncthreads();
   }
 
