@@ -180,11 +180,12 @@ __device__ __forceinline__ void se_block_store(uint8_t* p, int SW, uint32_t a, u
 //     transition table: EMPTY, and in a typical rule set the solids and liquids at rest;
 //     without one: EMPTY, which the shader itself leaves alone); the others are appended
 //     to a list of array offsets (a warp reserves its slots with one atomicAdd).  The
-//     blocks of a row past its last whole chunk are updated right there, and so are, in a
-//     tile reaching past the world, the chunks with cells outside it (block by block,
-//     those cells kept WALL); chunks wholly outside the world are left alone.
+//     blocks of a row past its last whole chunk are updated right there.  In a tile
+//     reaching past the world, chunks wholly outside it are left alone and chunks with
+//     cells outside it fill the list from its far end.
 //  2. se_chunk_process updates the listed chunks, one chunk per thread: with a table
-//     word-wide and with four independent lookups, else block by block with the rules.
+//     word-wide and with four independent lookups, else block by block with the rules;
+//     then the chunks with cells outside the world, block by block, those cells kept WALL.
 // Chunks are skipped whole, so the lanes that evaluate blocks do so together rather than
 // waiting on one another; blocks of one step are disjoint, so the list order is free.
 
