@@ -180,7 +180,9 @@ __device__ __forceinline__ float4 light_blend(const float4* sl, const uint8_t* s
     a1 = fadd(a1, t1);
     a2 = fadd(a2, t2);
     a3 = fadd(a3, falloff);
-    maxf = lmax<CLEAN>(falloff, maxf);
+    // clean: a == 0 leaves maxf (>= +0) as it is either way, so the running maximum need
+    // not wait for the falloff select
+    maxf = CLEAN ? fmaxf(a, maxf) : gmax(falloff, maxf);
     ++num;
     m0 = lmax<CLEAN>(m0, t0);  // the alpha of the maximum is not used (mix takes .rgb)
     m1 = lmax<CLEAN>(m1, t1);
