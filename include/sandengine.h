@@ -43,7 +43,8 @@ enum se_status {
   SE_ERR_BUFFER_TOO_SMALL = 13,
   SE_ERR_NOT_COMPILED = 14,   /* se_ruleset_compile has not succeeded yet */
   SE_ERR_BUDGET = 15,         /* serving: the request cannot fit the HBM budget */
-  SE_ERR_TIMEOUT = 16
+  SE_ERR_TIMEOUT = 16,
+  SE_ERR_CANCELLED = 17       /* serving: the request was withdrawn */
 };
 
 /* Modification shapes (sandengine-core/src/simulation.rs:41-42). */
@@ -178,6 +179,13 @@ int se_world_set_steps_per_launch(se_world* w, int k);
  * keeps the fastest; *best_k gets the chosen frames per launch.  (No counterpart in the
  * reference, which dispatches one frame at a time.) */
 int se_world_autotune(se_world* w, int reps, int* best_k);
+/* Chooses the compiled tile variant for multi-frame launches (k >= 2) or for one-frame
+ * launches (k = 1) directly: tile_w x tile_h output cells, up to k frames per launch.  An
+ * override of the autotuner, for profiling one variant.  (No counterpart in the reference.) */
+int se_world_set_tile(se_world* w, int tile_w, int tile_h, int k);
+/* The variant the next multi-frame launch uses (0, 0, 0 before the autotuner has run when
+ * it is to choose). */
+int se_world_get_tile(const se_world* w, int* tile_w, int* tile_h, int* k);
 /* Replace / read the grid (width*height uint32, row-major) from host memory.  Both
  * synchronize the world's stream. */
 int se_world_set_grid(se_world* w, const uint32_t* cells, size_t count);
@@ -223,7 +231,8 @@ int se_world_histogram(se_world* w, uint64_t* counts, int nbins);
  * SE_NOALLOC_MAX_BINS (257) 64-bit words, 2,056 bytes, which every GPU that loads the
  * library keeps until the process exits; nbins above 257 is rejected with
  * SE_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's device address
- * (make that first call before any stream capture).  Every call shares the array: it clears
+ * (make that first call before any stream capture); after a device reset (a new context on
+ * the device) the next call looks it up again.  Every call shares the array: it clears
  * the counters on `cuda_stream` (NULL = the legacy default stream), counts, copies nbins
  * counters to host_counts and synchronizes the stream before returning, so calls from one
  * thread never overlap; calls from different threads or streams that overlap on the GPU
@@ -292,6 +301,7 @@ typedef struct se_server_stats {
   long long iterations;        /* batched iterations (plain path: requests) */
   long long evictions, restores;
   long long peak_resident_bytes;
+  double restore_ms;           /* mean host time to bring an evicted session back into HBM */
 } se_server_stats;
 
 /* A server whose sessions' grids (two u32 buffers each) share one HBM arena of
@@ -305,18 +315,34 @@ int se_server_set_frames_per_iteration(se_server* s, int k);
 int se_server_open_session(se_server* s, int width, int height, const uint32_t* cells, int32_t frame,
                            int* session);
 int se_server_close_session(se_server* s, int session);
-/* Queues "advance nframes frames, applying mods to the first" for a session, arriving
- * arrival_ms after the start of the next run.  Requests of one session run in order. */
+/* Queues "advance nframes frames, applying mods to the first" for a session.  Requests of
+ * one session run in order.  Before se_server_run it arrives arrival_ms after the start of
+ * that run; while the live loop runs (se_server_start) it arrives when it is submitted and
+ * arrival_ms is ignored.  Safe to call from any thread while the live loop runs. */
 int se_server_submit(se_server* s, int session, int nframes, const se_modification* mods, int nmods,
                      double arrival_ms, int* request);
-/* Withdraws a submitted request that has not been run (cancelled before se_server_run):
- * the run skips it, its session does not advance for it, and its latency query fails. */
+/* Withdraws a submitted request that has not started: it is skipped, its session does not
+ * advance for it, and waiting for it returns SE_ERR_CANCELLED.  Any thread. */
 int se_server_cancel(se_server* s, int request);
-/* Serves every queued request in real time: requests are admitted when their arrival time
- * has passed and memory allows.  plain = 0: continuous batching (every active session
- * advances in one launch per iteration; sessions join and leave between iterations);
- * plain = 1: one request at a time, one launch per frame (the reference's dispatch). */
+/* Replay: serves every queued request in real time, admitting requests when their arrival
+ * time has passed and memory allows, and returns when all are done.  plain = 0: continuous
+ * batching (every active session advances in one launch per iteration; sessions join and
+ * leave between iterations); plain = 1: one request at a time, one launch per frame (the
+ * reference's dispatch). */
 int se_server_run(se_server* s, int plain);
+/* Live: starts the serving loop on a host thread of its own (plain as for se_server_run).
+ * Requests submitted from any thread are admitted at the loop's next iteration, while
+ * others are on the GPU, as sessions and HBM free up.  The reference's host likewise feeds
+ * edits into its running event loop (sandengine-core/src/lib.rs:57-69).  se_server_stop
+ * serves what was submitted, then ends the loop and returns its status. */
+int se_server_start(se_server* s, int plain);
+int se_server_stop(se_server* s);
+/* Blocks until the request has completed on the GPU (timeout_ms < 0: no limit), then gives
+ * its latency (completion minus submission).  SE_ERR_TIMEOUT when it has not completed in
+ * time, SE_ERR_CANCELLED for a withdrawn request.  se_server_poll does not block: *done = 1
+ * (and the latency) once completed, else 0.  Any thread. */
+int se_server_wait(se_server* s, int request, double timeout_ms, double* latency_ms);
+int se_server_poll(se_server* s, int request, int* done, double* latency_ms);
 int se_server_stats_get(se_server* s, se_server_stats* out);
 int se_server_request_latency(se_server* s, int request, double* latency_ms);
 int se_server_get_grid(se_server* s, int session, uint32_t* cells, size_t count);

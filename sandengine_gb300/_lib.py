@@ -16,7 +16,7 @@ SE_OK = 0
 STATUS_NAMES = {
     1: "InvalidArgument", 2: "MissingField", 3: "InvalidType", 4: "NotFound", 5: "NotRecognized",
     6: "Yaml", 7: "Panic", 8: "Glsl", 9: "Unsupported", 10: "Compile", 11: "Cuda", 12: "OutOfMemory",
-    13: "BufferTooSmall", 14: "NotCompiled", 15: "Budget", 16: "Timeout",
+    13: "BufferTooSmall", 14: "NotCompiled", 15: "Budget", 16: "Timeout", 17: "Cancelled",
 }
 PARSE_KINDS = {"MissingField", "InvalidType", "NotFound", "NotRecognized", "Yaml", "Panic", "Glsl",
                "Unsupported"}
@@ -93,6 +93,8 @@ _SIGS = {
     "se_world_histogram": ([_P, _P, _I], _I),
     "se_world_set_timing": ([_P, _I], _I),
     "se_world_autotune": ([_P, _I, ctypes.POINTER(_I)], _I),
+    "se_world_set_tile": ([_P, _I, _I, _I], _I),
+    "se_world_get_tile": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "se_grid_histogram_noalloc": ([_P, ctypes.c_uint64, _I, _P, _P], _I),
     "se_batch_create": ([_P, _I, _P, _P, ctypes.POINTER(_P)], _I),
     "se_batch_destroy": ([_P], None),
@@ -116,6 +118,10 @@ _SIGS = {
     "se_server_close_session": ([_P, _I], _I),
     "se_server_submit": ([_P, _I, _I, _P, _I, ctypes.c_double, ctypes.POINTER(_I)], _I),
     "se_server_run": ([_P, _I], _I),
+    "se_server_start": ([_P, _I], _I),
+    "se_server_stop": ([_P], _I),
+    "se_server_wait": ([_P, _I, ctypes.c_double, ctypes.POINTER(ctypes.c_double)], _I),
+    "se_server_poll": ([_P, _I, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double)], _I),
     "se_server_stats_get": ([_P, _P], _I),
     "se_server_cancel": ([_P, _I], _I),
     "se_server_request_latency": ([_P, _I, ctypes.POINTER(ctypes.c_double)], _I),

@@ -360,6 +360,41 @@ SE_API int se_world_set_steps_per_launch(se_world* w, int k) {
   });
 }
 
+SE_API int se_world_set_tile(se_world* w, int tile_w, int tile_h, int k) {
+  return guard([&] {
+    if (!w) return fail(SE_ERR_INVALID_ARGUMENT, "null world");
+    for (auto& t : se::rt::tile_variants())
+      if (t.tw == tile_w && t.th == tile_h && t.kmax == k) {
+        auto& W = *w->w;
+        if (k == 1) {
+          W.single = &t;
+        } else {
+          W.fused = &t;
+          W.steps_per_launch = 0;
+        }
+        return (int)SE_OK;
+      }
+    return fail(SE_ERR_INVALID_ARGUMENT, "no compiled tile variant " + std::to_string(tile_w) + "x" +
+                                             std::to_string(tile_h) + " with " + std::to_string(k) +
+                                             " frames per launch");
+  });
+}
+
+SE_API int se_world_get_tile(const se_world* w, int* tile_w, int* tile_h, int* k) {
+  return guard([&] {
+    if (!w || !tile_w || !tile_h || !k) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    const auto& W = *w->w;
+    const se::rt::TileVariant* v = W.steps_per_launch > 0 ? nullptr : W.fused;
+    if (!v)
+      for (auto& t : se::rt::tile_variants())
+        if (t.kmax >= std::max(1, W.steps_per_launch) && (!v || t.kmax < v->kmax)) v = &t;
+    *tile_w = v ? v->tw : 0;
+    *tile_h = v ? v->th : 0;
+    *k = v ? v->kmax : 0;
+    return (int)SE_OK;
+  });
+}
+
 namespace {
 int grid_copy(se_world* w, void* host, size_t count, bool to_device, bool sync) {
   if (!w || !host) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
@@ -703,13 +738,41 @@ SE_API int se_server_cancel(se_server* s, int request) {
 
 SE_API int se_server_request_latency(se_server* s, int request, double* latency_ms) {
   return guard([&] {
-    if (!s || !latency_ms || request < 0 || request >= (int)s->s->requests.size())
-      return fail(SE_ERR_INVALID_ARGUMENT, "bad request");
-    const auto& r = s->s->requests[(size_t)request];
-    if (r.cancelled) return fail(SE_ERR_INVALID_ARGUMENT, "request was cancelled");
-    if (r.done_ms < 0) return fail(SE_ERR_INVALID_ARGUMENT, "request has not been served");
-    *latency_ms = r.done_ms - r.arrival_ms;
-    return (int)SE_OK;
+    if (!s || !latency_ms) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(s->s->request_latency(request, latency_ms));
+  });
+}
+
+SE_API int se_server_start(se_server* s, int plain) {
+  return guard([&] {
+    if (!s) return fail(SE_ERR_INVALID_ARGUMENT, "null server");
+    return ret(s->s->start(plain != 0));
+  });
+}
+
+SE_API int se_server_stop(se_server* s) {
+  return guard([&] {
+    if (!s) return fail(SE_ERR_INVALID_ARGUMENT, "null server");
+    return ret(s->s->stop());
+  });
+}
+
+SE_API int se_server_wait(se_server* s, int request, double timeout_ms, double* latency_ms) {
+  return guard([&] {
+    if (!s) return fail(SE_ERR_INVALID_ARGUMENT, "null server");
+    bool done = false;
+    return ret(s->s->wait(request, timeout_ms, &done, latency_ms));
+  });
+}
+
+SE_API int se_server_poll(se_server* s, int request, int* done, double* latency_ms) {
+  return guard([&] {
+    if (!s || !done) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    bool d = false;
+    se::rt::Status st = s->s->wait(request, 0.0, &d, latency_ms);
+    *done = d ? 1 : 0;
+    if (st.code == SE_ERR_TIMEOUT) return (int)SE_OK;  // not done yet: *done = 0
+    return ret(st);
   });
 }
 
@@ -789,14 +852,14 @@ SE_API int se_world_load(se_world* w, const char* path) {
 
 SE_API int se_server_save_session(se_server* s, int session, const char* path) {
   return guard([&] {
-    if (!s || !path || session < 0 || session >= (int)s->s->sessions.size())
-      return fail(SE_ERR_INVALID_ARGUMENT, "bad argument");
-    const auto& ss = s->s->sessions[(size_t)session];
-    std::vector<uint32_t> cells((size_t)ss.W * ss.H);
-    se::rt::Status st = s->s->get_grid(session, cells.data(), cells.size());
+    if (!s || !path) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    int w = 0, h = 0;
+    int32_t frame = 0;
+    std::vector<uint32_t> cells;
+    se::rt::Status st = s->s->session_state(session, &w, &h, &frame, &cells);
     if (!st.ok()) return ret(st);
     std::string err;
-    if (!se::rt::snapshot_write(path, snapshot_header_for(*s->s->rs, ss.W, ss.H, ss.frame), cells.data(), &err))
+    if (!se::rt::snapshot_write(path, snapshot_header_for(*s->s->rs, w, h, frame), cells.data(), &err))
       return fail(SE_ERR_INVALID_ARGUMENT, err);
     return (int)SE_OK;
   });
@@ -817,9 +880,7 @@ SE_API int se_server_open_session_from(se_server* s, const char* path, int* sess
 
 SE_API int se_server_get_frame(se_server* s, int session, int32_t* frame) {
   return guard([&] {
-    if (!s || !frame || session < 0 || session >= (int)s->s->sessions.size())
-      return fail(SE_ERR_INVALID_ARGUMENT, "bad session");
-    *frame = s->s->sessions[(size_t)session].frame;
-    return (int)SE_OK;
+    if (!s || !frame) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(s->s->session_state(session, nullptr, nullptr, frame, nullptr));
   });
 }

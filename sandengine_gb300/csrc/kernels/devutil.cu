@@ -83,32 +83,70 @@ cudaError_t grid_histogram(const uint32_t* g, unsigned long long n, int nbins, u
 
 int noalloc_max_bins() { return SE_NOALLOC_MAX_BINS; }
 
+namespace {
+// The driver's id of the calling thread's current context (cuCtxGetCurrent, cuCtxGetId),
+// reached through the runtime's entry-point query, so the library still needs no link to
+// the driver library.  False when the driver does not offer them.
+bool current_context_id(unsigned long long* id) {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  void* ctx = nullptr;
+  return get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, id) == 0;
+}
+}  // namespace
+
 // The histogram of grid_histogram, counted in se_noalloc_hist instead of caller- or
 // library-allocated memory.  The host must not pass the array's name to a kernel (in host
-// code it is a stand-in, not a device address), so the device address is looked up once
-// per device, with that device current, and cached.  The counters are cleared on the
-// stream before each use; the results are copied to host_counts and the stream is
-// synchronized before returning.
+// code it is a stand-in, not a device address), so its device address is looked up with
+// the device current (set-up on the first call on a device) and cached per device, tagged
+// with the id of the context it was looked up in: after a device reset (a new primary
+// context) the next call looks it up again.  The counters are cleared on the stream
+// before each use; the results are copied to host_counts and the stream is synchronized
+// before returning.
 cudaError_t histogram_noalloc(const uint32_t* g, unsigned long long n, int nbins, unsigned long long* host_counts,
                               cudaStream_t s) {
   constexpr int kMaxDevices = 64;
-  static unsigned long long* addr[kMaxDevices] = {};
+  struct Slot {
+    unsigned long long* addr = nullptr;
+    unsigned long long ctx_id = 0;
+  };
+  static Slot slots[kMaxDevices];
   static std::mutex mu;
   if (nbins < 1 || nbins > SE_NOALLOC_MAX_BINS) return cudaErrorInvalidValue;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  e = cudaSetDevice(dev);  // makes the device's primary context current on this thread
+  if (e != cudaSuccess) return e;
+  unsigned long long ctx = 0;
+  const bool have_ctx = current_context_id(&ctx);
   unsigned long long* p = nullptr;
   {
     std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
+    Slot& sl = slots[dev];
+    if (!sl.addr || (have_ctx && sl.ctx_id != ctx)) {
       void* q = nullptr;
       e = cudaGetSymbolAddress(&q, se_noalloc_hist);
       if (e != cudaSuccess) return e;
-      addr[dev] = static_cast<unsigned long long*>(q);
+      sl.addr = static_cast<unsigned long long*>(q);
+      sl.ctx_id = have_ctx ? ctx : 0;
     }
-    p = addr[dev];
+    p = sl.addr;
   }
   e = cudaMemsetAsync(p, 0, sizeof(unsigned long long) * (size_t)nbins, s);
   if (e != cudaSuccess) return e;

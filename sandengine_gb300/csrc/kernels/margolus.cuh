@@ -112,6 +112,7 @@ extern "C" __global__ void __launch_bounds__(256) se_build_static(uint16_t* __re
   }
   st[w] = word;
 }
+
 #endif
 
 // Index checks of the CHECKED build (module compiled with SE_CHECKED): a failed check sets
@@ -380,11 +381,31 @@ __device__ __forceinline__ void se_chunk_eval(uint8_t* p, int SW, uint32_t x, co
 }
 #endif
 
-template <int SW, int SH, int OX, int NT>
-__device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int nb,
-                                                 int gx0, int gy0, int f, int W, int H,
-                                                 const uint16_t* __restrict__ lut) {
+// The chunks with cells outside the world (edge tiles), from the far end of the chunk list,
+// block by block with those cells kept WALL.
+template <int SW, int SH, int NT>
+__device__ __forceinline__ void se_border_process(uint8_t* sm, const uint16_t* __restrict__ list, int nb, int gx0,
+                                                  int gy0, int f, int W, int H, const uint16_t* __restrict__ lut) {
   constexpr int CAP = (SW / 8) * (SH / 2);
+  for (int i = threadIdx.x; i < nb; i += NT) {
+    if (!se_check(i < CAP, 4u)) break;
+    const int off = list[CAP - 1 - i];
+    if (!se_check(off + SW + 7 < SW * SH, 8u)) continue;
+    const int ly = off / SW, lx = off - ly * SW;
+    for (int kb = 0; kb < 4; ++kb) {
+      uint8_t* p = sm + off + 2 * kb;
+      uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+      if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
+      const int gx = gx0 + lx + 2 * kb, gy = gy0 + ly;
+      se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
+      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, true);
+    }
+  }
+}
+
+template <int SW, int SH, int OX, int NT>
+__device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int gx0,
+                                                 int gy0, int f, int W, int H, const uint16_t* __restrict__ lut) {
   const uint32_t xf = (uint32_t)f * 4541161u;
   for (int i = threadIdx.x; i < n; i += NT) {
     if (!se_check(i < (SW / 8) * (SH / 2), 4u)) break;
@@ -407,21 +428,6 @@ __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __
       p[SW + 1] = (uint8_t)d;
     }
 #endif
-  }
-  // chunks with cells outside the world (edge tiles), from the far end of the list
-  for (int i = threadIdx.x; i < nb; i += NT) {
-    if (!se_check(i < CAP, 4u)) break;
-    const int off = list[CAP - 1 - i];
-    if (!se_check(off + SW + 7 < SW * SH, 8u)) continue;
-    const int ly = off / SW, lx = off - ly * SW;
-    for (int kb = 0; kb < 4; ++kb) {
-      uint8_t* p = sm + off + 2 * kb;
-      uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
-      if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
-      const int gx = gx0 + lx + 2 * kb, gy = gy0 + ly;
-      se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
-      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, true);
-    }
   }
 }
 
@@ -535,6 +541,72 @@ __device__ __forceinline__ void se_store_region(const uint8_t* sm, int SW, int h
   }
 }
 
+// ---- modification (edit) records ------------------------------------------------------
+// One 32-byte SimModification record (sandengine-core/src/simulation.rs:45-56), with
+// mod_matID already mapped through getMaterialFromID (unknown ids -> NULL) by the host.
+struct SeMod {
+  int px, py, shape, size, mat, pad0, pad1, pad2;
+};
+
+// falling_sand.glsl:143-160 for one mod and one cell.
+__device__ __forceinline__ bool se_mod_hits(const SeMod& m, int x, int y) {
+  const int dx = se_iabs((int)((unsigned)m.px - (unsigned)x));
+  const int dy = se_iabs((int)((unsigned)m.py - (unsigned)y));
+  if (m.shape == 0) {  // MODSHAPE_CIRCLE: sqrt(pow(dx,2) + pow(dy,2)) <= size in binary32
+    const float fx = __int2float_rn(dx), fy = __int2float_rn(dy);
+    const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)));
+    return dist <= __int2float_rn(m.size);
+  }
+  if (m.shape == 1) return dx <= m.size && dy <= m.size;  // MODSHAPE_SQUARE
+  return false;
+}
+
+// The edit pass runs after the frame's block update, on the updated grid: a cell hit by
+// any mod ends with the material of the LAST mod that hits it, unless that material is
+// NULL (falling_sand.glsl:134-179); other cells keep their simulated value.  Thread t
+// handles one cell of mod q's bounding box (boxes[q] = x0, y0, x1, y1 inclusive, clipped
+// to the world; starts[q] = first thread of mod q) and writes only if q is the last mod
+// hitting it.  The mod list travels in the kernel's parameter space (14 KB).
+struct SeEditParams {
+  SeMod mods[256];
+  int4 boxes[256];
+  long long starts[257];
+};
+
+// The edit pass inside a tile launch, after the block update of its first frame: every
+// array cell of the world (and of the buffer rows [ya, yb)) hit by a mod of `p` takes the
+// material of the last mod hitting it unless that material is NULL (the rule of se_edit
+// below, falling_sand.glsl:134-179).  Block partners were updated from the pre-edit values,
+// as every invocation of the reference's frame reads the input texture.  Mods are visited
+// in order; a cell is written only by the last mod that hits it, so no two threads write
+// one cell and the mods need no barrier between them.
+__device__ __forceinline__ void se_tile_edits(uint8_t* sm, int SW, int SH, int gx0, int gy0, int W, int H, int ya,
+                                              int yb, const SeEditParams* __restrict__ p, int n, int nt) {
+  const int rx0 = gx0 > 0 ? gx0 : 0, rx1 = (gx0 + SW < W ? gx0 + SW : W) - 1;
+  const int ylo = ya > 0 ? ya : 0, yhi = yb < H ? yb : H;
+  const int ry0 = gy0 > ylo ? gy0 : ylo, ry1 = (gy0 + SH < yhi ? gy0 + SH : yhi) - 1;
+  for (int q = 0; q < n; ++q) {
+    const int4 b = p->boxes[q];
+    if (p->mods[q].mat == (int)SE_NULL) continue;  // its cells keep the simulated value
+    const int x0 = b.x > rx0 ? b.x : rx0, x1 = b.z < rx1 ? b.z : rx1;
+    const int y0 = b.y > ry0 ? b.y : ry0, y1 = b.w < ry1 ? b.w : ry1;
+    if (x0 > x1 || y0 > y1) continue;
+    const SeMod m = p->mods[q];
+    const int w = x1 - x0 + 1, cnt = w * (y1 - y0 + 1);
+    for (int t = threadIdx.x; t < cnt; t += nt) {
+      const int y = y0 + t / w, x = x0 + t % w;
+      if (!se_mod_hits(m, x, y)) continue;
+      bool later = false;
+      for (int r = q + 1; r < n && !later; ++r) {
+        const int4 rb = p->boxes[r];
+        later = x >= rb.x && x <= rb.z && y >= rb.y && y <= rb.w && se_mod_hits(p->mods[r], x, y);
+      }
+      const int i = (y - gy0) * SW + (x - gx0);
+      if (!later && se_check(i >= 0 && i < SW * SH, 32u)) sm[i] = (uint8_t)m.mat;
+    }
+  }
+}
+
 // Advances the tile with top-left cell (X0, Y0) of a W x H world by k <= KMAX frames whose
 // counters are f0, f0+1, ... (all >= 2; the host handles the frame-1 clear).
 // src and dst hold the world rows [ya, yb) (row gy at (gy - ya) * W): the whole world, or a
@@ -545,7 +617,8 @@ __device__ __forceinline__ void se_store_region(const uint8_t* sm, int SW, int h
 template <int TW, int TH, int KMAX, int NT>
 __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W,
                                             int H, int f0, int k, const uint16_t* __restrict__ lut, int X0, int Y0,
-                                            int ya, int yb) {
+                                            int ya, int yb, const SeEditParams* __restrict__ edits = nullptr,
+                                            int nedits = 0) {
   constexpr int HX = ((KMAX + 3) / 4) * 4, HY = KMAX;
   constexpr int SW = TW + 2 * HX, SH = TH + 2 * HY, WPR = SW / 4;
   static_assert(TW % 4 == 0, "tile width must be a multiple of 4");
@@ -646,10 +719,15 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
     const int n = *c, nb = *bc;
     if (threadIdx.x == 0) cnt[(s + 1) & 1] = cnt[2 + ((s + 1) & 1)] = 0;  // last read in step s - 1
     if (se_off_x(f) == 0)
-      se_chunk_process<SW, SH, 0, NT>(sm, list, n, nb, gx0, gy0, f, W, H, lut);
+      se_chunk_process<SW, SH, 0, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
     else
-      se_chunk_process<SW, SH, 1, NT>(sm, list, n, nb, gx0, gy0, f, W, H, lut);
+      se_chunk_process<SW, SH, 1, NT>(sm, list, n, gx0, gy0, f, W, H, lut);
+    se_border_process<SW, SH, NT>(sm, list, nb, gx0, gy0, f, W, H, lut);
     __syncthreads();
+    if (s == 0 && nedits > 0) {  // the first frame's edits (the host passes them only then)
+      se_tile_edits(sm, SW, SH, gx0, gy0, W, H, ya, yb, edits, nedits, NT);
+      __syncthreads();
+    }
   }
 
   constexpr int OWPR = TW / 4;
@@ -672,11 +750,15 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
 
 // One world, or the band of world rows [ya, yb) held by src and dst: the tile is
 // (blockIdx.x, blockIdx.y) counted from row ya.
+// With `edits`, the first frame's edit pass runs inside the launch (se_tile_edits).
 template <int TW, int TH, int KMAX, int NT>
 __device__ __forceinline__ void se_tile_impl(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W,
-                                             int H, int f0, int k, const uint16_t* __restrict__ lut, int ya, int yb) {
+                                             int H, int f0, int k, const uint16_t* __restrict__ lut, int ya, int yb,
+                                             const SeEditParams* __restrict__ edits = nullptr, int nedits = 0) {
   if (ya < 0 || yb > H || ya >= yb || k < 1 || k > KMAX) return;  // the host validates these too
-  se_tile_run<TW, TH, KMAX, NT>(src, dst, W, H, f0, k, lut, blockIdx.x * TW, ya + blockIdx.y * TH, ya, yb);
+  if (nedits < 0 || nedits > 256) return;
+  se_tile_run<TW, TH, KMAX, NT>(src, dst, W, H, f0, k, lut, blockIdx.x * TW, ya + blockIdx.y * TH, ya, yb, edits,
+                                nedits);
 }
 
 // ---- many worlds -------------------------------------------------------------------------
@@ -769,37 +851,6 @@ extern "C" __global__ void __launch_bounds__(256) se_batch_finalize(SeWorldDesc*
 }
 
 // ---- modification (edit) pass ------------------------------------------------------------
-// One 32-byte SimModification record (sandengine-core/src/simulation.rs:45-56), with
-// mod_matID already mapped through getMaterialFromID (unknown ids -> NULL) by the host.
-struct SeMod {
-  int px, py, shape, size, mat, pad0, pad1, pad2;
-};
-
-// falling_sand.glsl:143-160 for one mod and one cell.
-__device__ __forceinline__ bool se_mod_hits(const SeMod& m, int x, int y) {
-  const int dx = se_iabs((int)((unsigned)m.px - (unsigned)x));
-  const int dy = se_iabs((int)((unsigned)m.py - (unsigned)y));
-  if (m.shape == 0) {  // MODSHAPE_CIRCLE: sqrt(pow(dx,2) + pow(dy,2)) <= size in binary32
-    const float fx = __int2float_rn(dx), fy = __int2float_rn(dy);
-    const float dist = __fsqrt_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)));
-    return dist <= __int2float_rn(m.size);
-  }
-  if (m.shape == 1) return dx <= m.size && dy <= m.size;  // MODSHAPE_SQUARE
-  return false;
-}
-
-// The edit pass runs after the frame's block update, on the updated grid: a cell hit by
-// any mod ends with the material of the LAST mod that hits it, unless that material is
-// NULL (falling_sand.glsl:134-179); other cells keep their simulated value.  Thread t
-// handles one cell of mod q's bounding box (boxes[q] = x0, y0, x1, y1 inclusive, clipped
-// to the world; starts[q] = first thread of mod q) and writes only if q is the last mod
-// hitting it.  The mod list travels in the kernel's parameter space (14 KB).
-struct SeEditParams {
-  SeMod mods[256];
-  int4 boxes[256];
-  long long starts[257];
-};
-
 // grid holds world rows from row0 on (the boxes lie within them).
 extern "C" __global__ void __launch_bounds__(256) se_edit(uint32_t* __restrict__ grid, int W, int H, int nmods,
                                                           long long total, const SeEditParams p, int row0) {

@@ -210,26 +210,29 @@ Status World::autotune(int reps, int* best_k) {
 }
 
 Status launch_tile_kernel(const Ruleset& rs, const TileVariant& v, const uint32_t* src, uint32_t* dst, int W, int H,
-                          int f0, int k, int ya, int yb, cudaStream_t stream) {
+                          int f0, int k, int ya, int yb, cudaStream_t stream, const EditParams* edits, int nedits) {
   if (v.kmax < k || k < 1) return {SE_ERR_INVALID_ARGUMENT, "no kernel variant for this many frames per launch"};
   if (ya < 0 || yb > H || ya >= yb) return {SE_ERR_INVALID_ARGUMENT, "tile rows outside the world"};
-  cudaKernel_t kern = rs.module->get(v.name());
+  if (edits && (nedits < 1 || nedits > SE_MAX_MODIFICATIONS))
+    return {SE_ERR_INVALID_ARGUMENT, "an edit launch takes 1..256 modifications"};
+  cudaKernel_t kern = rs.module->get(edits ? v.edit_name() : v.name());
   const uint16_t* lut = rs.d_lut;
-  void* args[] = {(void*)&src, (void*)&dst, &W, &H, &f0, &k, (void*)&lut, &ya, &yb};  // se_tile_impl's order
+  // se_tile_impl's order; the edit variant adds the edit list (by value) and its length
+  void* args[] = {(void*)&src, (void*)&dst, &W, &H, &f0, &k, (void*)&lut, &ya, &yb, (void*)edits, &nedits};
   dim3 grid((unsigned)((W + v.tw - 1) / v.tw), (unsigned)((yb - ya + v.th - 1) / v.th));
   SE_CUDA(cudaLaunchKernel((const void*)kern, grid, dim3((unsigned)v.nt), args, tile_smem_bytes(v, rs.lut_shape()),
                            stream));
   return Status::Ok();
 }
 
-Status World::launch_tiles(int f0, int k, const TileVariant* v, bool commit) {
+Status World::launch_tiles(int f0, int k, const TileVariant* v, bool commit, const EditParams* edits, int nedits) {
   if (!v || v->kmax < k) return {SE_ERR_INVALID_ARGUMENT, "no kernel variant for this many frames per launch"};
   Timed* t = nullptr;
   if (timing) {
     Status s = timing_begin(0, (long long)W * H, k, &t);
     if (!s.ok()) return s;
   }
-  Status s = launch_tile_kernel(*rs, *v, buf[cur], buf[cur ^ 1], W, wh, f0, k, ya, ya + H, stream);
+  Status s = launch_tile_kernel(*rs, *v, buf[cur], buf[cur ^ 1], W, wh, f0, k, ya, ya + H, stream, edits, nedits);
   if (!s.ok()) return s;
   if (t) SE_CUDA(cudaEventRecord(t->b, stream));
   if (commit) cur ^= 1;
@@ -274,13 +277,9 @@ Status World::timing_read(int pass, double* ms, long long* launches, long long* 
   return Status::Ok();
 }
 
-Status World::launch_edit(const se_modification* mods, int nlive) {
-  return launch_edit_on(*rs, buf[cur], W, ya, H, mods, nlive, stream);
-}
-
-Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int row0, int rows, const se_modification* mods,
-                      int nlive, cudaStream_t stream) {
-  EditParams p;
+long long fill_edit_params(const Ruleset& rs, int W, int row0, int rows, const se_modification* mods, int nlive,
+                           EditParams* out) {
+  EditParams& p = *out;
   memset(&p, 0, sizeof p);
   long long total = 0;
   const int nmat = rs.num_materials();
@@ -311,14 +310,21 @@ Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int row0, int ro
       p.box[4 * i + 2] = (int)x1;
       p.box[4 * i + 3] = (int)y1;
       total += (x1 - x0 + 1) * (y1 - y0 + 1);
-    } else {
+    } else {  // empty: x1 < x0
       p.box[4 * i + 0] = 0;
       p.box[4 * i + 1] = 0;
-      p.box[4 * i + 2] = 0;
-      p.box[4 * i + 3] = 0;
+      p.box[4 * i + 2] = -1;
+      p.box[4 * i + 3] = -1;
     }
   }
   p.start[nlive] = total;
+  return total;
+}
+
+Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int row0, int rows, const se_modification* mods,
+                      int nlive, cudaStream_t stream) {
+  EditParams p;
+  long long total = fill_edit_params(rs, W, row0, rows, mods, nlive, &p);
   if (total == 0) return Status::Ok();
   cudaKernel_t kern = rs.module->get("se_edit");
   uint32_t* g = grid;
@@ -343,7 +349,7 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
   if (steps_per_launch > 0) {
     vmulti = pick_variant(steps_per_launch);
   } else {
-    if (!fused && nframes - (nlive > 0 ? 1 : 0) >= 2) {
+    if (!fused && nframes >= 2) {
       Status s = autotune(2, nullptr);
       if (!s.ok()) return s;
     }
@@ -357,13 +363,13 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
       if (f == 1) {  // the clear goes to the spare buffer: the light pass reads the old grid
         SE_CUDA(cudaMemsetAsync(buf[cur ^ 1], 0, (size_t)W * H * sizeof(uint32_t), stream));
         cur ^= 1;
+      } else if (i == 0 && nlive > 0) {  // the frame and its edit pass in one launch
+        fill_edit_params(*rs, W, ya, H, mods, nlive, &edit_params);
+        Status s = launch_tiles(f, 1, vone, true, &edit_params, nlive);
+        if (!s.ok()) return s;
       } else {
         Status s = launch_tiles(f, 1, vone);
         if (!s.ok()) return s;
-        if (i == 0 && nlive > 0) {
-          s = launch_edit(mods, nlive);
-          if (!s.ok()) return s;
-        }
       }
       Status s = light_frame();
       if (!s.ok()) return s;
@@ -379,16 +385,16 @@ Status World::step(int nframes, const se_modification* mods, int nmods) {
       ++i;
       continue;
     }
-    if (i == 0 && nlive > 0) {
-      Status s = launch_tiles(f, 1, vone);
+    const int k = std::min(kdef, nframes - i);
+    const TileVariant* v = k == 1 ? vone : vmulti;
+    if (i == 0 && nlive > 0) {  // the edit pass runs inside the launch, after its first frame
+      fill_edit_params(*rs, W, ya, H, mods, nlive, &edit_params);
+      Status s = launch_tiles(f, k, v, true, &edit_params, nlive);
       if (!s.ok()) return s;
-      s = launch_edit(mods, nlive);
-      if (!s.ok()) return s;
-      ++i;
+      i += k;
       continue;
     }
-    const int k = std::min(kdef, nframes - i);
-    Status s = launch_tiles(f, k, k == 1 ? vone : vmulti);
+    Status s = launch_tiles(f, k, v);
     if (!s.ok()) return s;
     i += k;
   }

@@ -86,11 +86,12 @@ struct World {
   Status step(int nframes, const se_modification* mods, int nmods);
   // k frames with counters f0.. from buf[cur] into buf[cur^1]; commit=false leaves cur
   // (the world's state) unchanged, for tuning trials.
-  Status launch_tiles(int f0, int k, const TileVariant* v, bool commit = true);
+  Status launch_tiles(int f0, int k, const TileVariant* v, bool commit = true, const EditParams* edits = nullptr,
+                      int nedits = 0);
   // Times every tile variant on this world (without changing it) and keeps the fastest
   // multi-frame and one-frame variants.  *best_k gets the chosen frames per launch.
   Status autotune(int reps, int* best_k);
-  Status launch_edit(const se_modification* mods, int nlive);
+  EditParams edit_params;  // the edit list of the current step's first launch (copied at launch)
   int default_k() const;
   // Opt-in per-launch CUDA-event timing (for roofline measurements) of the tile kernel
   // (pass 0), the light pass (1), the colour pass (2) and the composite (3, its pyramid
@@ -145,8 +146,17 @@ struct World {
 // One launch of a single-world tile kernel (se_tile_*): k frames with counters f0.. over
 // the world rows [ya, yb) of a W x H world held by src / dst (the whole world: 0, H).  The
 // one place that builds this kernel's argument list.
+// With `edits` (nedits live mods), the edit pass of the first frame runs inside the launch
+// (se_tile_edit_*).
 Status launch_tile_kernel(const Ruleset& rs, const TileVariant& v, const uint32_t* src, uint32_t* dst, int W, int H,
-                          int f0, int k, int ya, int yb, cudaStream_t stream);
+                          int f0, int k, int ya, int yb, cudaStream_t stream, const EditParams* edits = nullptr,
+                          int nedits = 0);
+
+// The edit pass inputs for `nlive` mods over world rows [row0, row0 + rows) of a W-wide
+// world: records with their materials mapped through getMaterialFromID and the bounding
+// boxes of the cells each can hit (empty boxes have x1 < x0).  Returns the box cells.
+long long fill_edit_params(const Ruleset& rs, int W, int row0, int rows, const se_modification* mods, int nlive,
+                           EditParams* p);
 
 // The edit pass (se_edit) for `nlive` mods over world rows [row0, row0 + rows) of a W-wide
 // world, held by `grid`.

@@ -19,6 +19,10 @@ std::string TileVariant::name() const {
   return "se_tile_" + std::to_string(tw) + "x" + std::to_string(th) + "_k" + std::to_string(kmax);
 }
 
+std::string TileVariant::edit_name() const {
+  return "se_tile_edit_" + std::to_string(tw) + "x" + std::to_string(th) + "_k" + std::to_string(kmax);
+}
+
 // Tile shapes and fusion depths compiled into every rule-set module; the launcher and the
 // autotuner choose among them.  Larger tiles recompute a smaller share of halo cells per
 // fused step (128x64 at k=8: 1.41x the tile's cells; 256x128 at k=8: 1.20x).  The shared
@@ -42,6 +46,13 @@ std::string kernel_source(const std::string& generated_rules) {
          " const uint16_t* __restrict__ lut, int ya, int yb) {\n"
       << "  se_tile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
       << ">(src, dst, W, H, f0, k, lut, ya, yb);\n}\n";
+    // the edit list travels in the parameter space, read in place (__grid_constant__)
+    o << "extern \"C\" __global__ void __launch_bounds__(" << t.nt << ") " << t.edit_name()
+      << "(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int W, int H, int f0, int k,"
+         " const uint16_t* __restrict__ lut, int ya, int yb, const __grid_constant__ SeEditParams edits,"
+         " int nedits) {\n"
+      << "  se_tile_impl<" << t.tw << ", " << t.th << ", " << t.kmax << ", " << t.nt
+      << ">(src, dst, W, H, f0, k, lut, ya, yb, &edits, nedits);\n}\n";
     o << "extern \"C\" __global__ void __launch_bounds__(" << t.nt << ") " << t.multi_name()
       << "(const SeWorldDesc* __restrict__ worlds, const SeTileJob* __restrict__ jobs, int pass,"
          " int frames_done, int k, const uint16_t* __restrict__ lut) {\n"
@@ -185,6 +196,7 @@ bool Module::load(const std::string& cubin, const LutShape& lut, std::string* er
   }
   for (auto& t : tile_variants()) {
     names.push_back(t.name());
+    names.push_back(t.edit_name());
     names.push_back(t.multi_name());
     names.push_back(t.serve_name());
   }
@@ -198,7 +210,7 @@ bool Module::load(const std::string& cubin, const LutShape& lut, std::string* er
     kernels[n] = k;
   }
   for (auto& t : tile_variants()) {
-    for (const std::string& n : {t.name(), t.multi_name(), t.serve_name()}) {
+    for (const std::string& n : {t.name(), t.edit_name(), t.multi_name(), t.serve_name()}) {
       e = cudaFuncSetAttribute((const void*)kernels[n], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)tile_smem_bytes(t, lut));
       if (e != cudaSuccess) {

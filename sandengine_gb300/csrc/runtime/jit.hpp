@@ -14,6 +14,7 @@ namespace se::rt {
 struct TileVariant {
   int tw, th, kmax, nt;
   std::string name() const;        // single-world kernel
+  std::string edit_name() const;   // single-world kernel with the first frame's edit pass
   std::string multi_name() const;  // many-world (tile job list) kernel
   std::string serve_name() const;  // serving iteration kernel (per-world frame counts)
   int halo_x() const { return ((kmax + 3) / 4) * 4; }

@@ -4,9 +4,13 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
+#include <condition_variable>
 #include <deque>
 #include <map>
 #include <memory>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../../include/sandengine.h"
@@ -15,6 +19,15 @@
 
 namespace se::rt {
 
+// Two ways to serve:
+//  * replay (run): every request queued before the call, each with an arrival time; the call
+//    serves them in real time and returns when all are done;
+//  * live (start ... stop): a loop on its own host thread serves requests as they are
+//    submitted, from any thread, until stop.  A request's arrival is the moment it is
+//    submitted; wait / poll report its completion.
+// Both run the same scheduler (serve_batched / serve_plain).  Every member the loop and the
+// API calls share is guarded by `mu`; the loop never holds a reference into `sessions` or
+// `requests` across a point where it releases the lock (other threads may append to them).
 struct Server {
   struct Session {
     int W = 0, H = 0;
@@ -38,9 +51,10 @@ struct Server {
     double arrival_ms = 0;
     bool started = false;
     bool cancelled = false;  // withdrawn before it started (se_server_cancel)
-    long long iter = -1;  // iteration that completed it
-    double done_ms = -1;
+    bool done = false;       // its last frame has completed on the GPU
+    double done_ms = -1;     // completion time on the GPU, from the run's time origin
   };
+  using Clock = std::chrono::steady_clock;
 
   std::shared_ptr<Ruleset> rs;
   size_t budget = 0;
@@ -49,7 +63,7 @@ struct Server {
   size_t used = 0, peak_used = 0;
   std::vector<Session> sessions;
   std::vector<Request> requests;
-  size_t first_pending = 0;   // requests before this index have been served
+  size_t first_pending = 0;   // replay: requests before this index have been served
   size_t last_run_begin = 0;  // first request of the last run
   const TileVariant* variant = nullptr;
   cudaStream_t stream = nullptr;
@@ -63,10 +77,31 @@ struct Server {
     WorldDesc* d_desc = nullptr;
     int* d_prefix = nullptr;
   } ring[kRing];
-  std::vector<cudaEvent_t> iter_events;
+  // The run's time origin (an event and the host clock read when it completed), and the
+  // iterations in flight: each records an event, with the requests it completes.
+  cudaEvent_t t0 = nullptr;
+  Clock::time_point host_t0;
+  struct Inflight {
+    cudaEvent_t ev;
+    std::vector<int> completes;
+  };
+  std::deque<Inflight> inflight;
+  std::vector<cudaEvent_t> event_pool;
   long long iterations = 0, evictions = 0, restores = 0;
   double cell_updates = 0;
   double wall_ms = 0;
+  double restore_ms_total = 0;  // host time spent restoring evicted sessions
+
+  // live loop
+  std::mutex mu;
+  std::condition_variable cv_work;  // the loop waits here for submissions
+  std::condition_variable cv_done;  // wait() waits here for completions
+  std::thread loop;
+  bool live = false, stopping = false;
+  bool loop_running = false;
+  int device = 0;  // the device the server was created on (its loop thread selects it)
+  Status loop_status;    // the loop's first failure (then it stops serving)
+  std::deque<int> inbox;  // live: submitted requests not yet admitted, in arrival order
 
   ~Server();
   Status create(std::shared_ptr<Ruleset> r, long long budget_bytes);
@@ -74,11 +109,17 @@ struct Server {
   Status open_session(int w, int h, const uint32_t* cells, int32_t frame, int* id);
   Status close_session(int id);
   Status submit(int session, int nframes, const se_modification* mods, int nmods, double arrival_ms, int* id);
-  // Withdraws a request that has not been run yet: the next run skips it and its session's
-  // frame counter does not move for it.
+  // Withdraws a request that has not started: it is skipped and its session's frame counter
+  // does not move for it.
   Status cancel(int request);
-  Status run(bool plain);
+  Status run(bool plain);  // replay
+  Status start(bool plain);  // live
+  Status stop();            // live: serves what was submitted, then ends the loop
+  // Waits up to timeout_ms (< 0: no limit) for a request; *done tells whether it completed.
+  Status wait(int request, double timeout_ms, bool* done, double* latency_ms);
+  Status request_latency(int request, double* latency_ms);
   Status get_grid(int session, uint32_t* host, size_t count);
+  Status session_state(int session, int* w, int* h, int32_t* frame, std::vector<uint32_t>* cells);
   Status stats(se_server_stats* out);
 
  private:
@@ -86,9 +127,16 @@ struct Server {
   void release(size_t off, size_t bytes);
   Status make_resident(int s, bool* ok);
   Status evict(int s);
-  Status run_batched();
-  Status run_plain();
+  Status begin_run();
+  Status serve_batched(std::unique_lock<std::mutex>& lk);
+  Status serve_plain(std::unique_lock<std::mutex>& lk);
   Status stage_reserve(Stage& st, size_t n);
+  Status record_iteration(std::vector<int> completes);
+  // Retires finished iterations (all of them when `all`, waiting for the GPU with the lock
+  // released), stamping their requests' completion times.
+  Status retire(std::unique_lock<std::mutex>& lk, bool all);
+  Status throttle(std::unique_lock<std::mutex>& lk, size_t max_inflight);
+  Status get_grid_locked(int session, uint32_t* host, size_t count);
 };
 
 }  // namespace se::rt

@@ -1,10 +1,19 @@
 """Serving simulation sessions with continuous batching (no counterpart in the reference).
 
+Replay (a recorded trace of requests with arrival times):
+
     srv = Server(ruleset, budget_bytes=150 << 30)
     s = srv.open_session(w, h, cells=None, frame=1)
     r = srv.submit(s, nframes=300, mods=[SimModification(...)], arrival_ms=12.5)
     srv.run()              # continuous batching; srv.run(plain=True): one request at a time
     srv.stats()            # p50/p99 latency, throughput, evictions
+
+Live (requests submitted from any thread while the loop runs):
+
+    srv.start()            # the serving loop on its own host thread
+    r = srv.submit(s, 300) # arrives now; admitted at the loop's next iteration
+    srv.wait(r)            # latency in ms once it has completed on the GPU
+    srv.stop()
 """
 from __future__ import annotations
 
@@ -23,7 +32,7 @@ class ServerStats(ctypes.Structure):
                 ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("wall_ms", ctypes.c_double),
                 ("cell_updates", ctypes.c_double), ("iterations", ctypes.c_longlong),
                 ("evictions", ctypes.c_longlong), ("restores", ctypes.c_longlong),
-                ("peak_resident_bytes", ctypes.c_longlong)]
+                ("peak_resident_bytes", ctypes.c_longlong), ("restore_ms", ctypes.c_double)]
 
 
 class Server:
@@ -81,6 +90,27 @@ class Server:
 
     def run(self, plain: bool = False) -> None:
         check(lib().se_server_run(self._h, 1 if plain else 0))
+
+    def start(self, plain: bool = False) -> None:
+        """Start the live serving loop (its own host thread)."""
+        check(lib().se_server_start(self._h, 1 if plain else 0))
+
+    def stop(self) -> None:
+        """Serve what was submitted, then end the live loop."""
+        check(lib().se_server_stop(self._h))
+
+    def wait(self, request: int, timeout_ms: float = -1.0) -> float:
+        """Block until the request has completed on the GPU; returns its latency in ms.
+        Raises SandengineError (kind Timeout) when timeout_ms passes first."""
+        v = ctypes.c_double()
+        check(lib().se_server_wait(self._h, int(request), float(timeout_ms), ctypes.byref(v)))
+        return v.value
+
+    def poll(self, request: int) -> Optional[float]:
+        """The request's latency in ms once it has completed, else None (does not block)."""
+        d, v = ctypes.c_int(), ctypes.c_double()
+        check(lib().se_server_poll(self._h, int(request), ctypes.byref(d), ctypes.byref(v)))
+        return v.value if d.value else None
 
     def stats(self) -> dict:
         st = ServerStats()

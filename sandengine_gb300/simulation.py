@@ -143,6 +143,17 @@ class Simulation:
         """Replace the grid and frame counter from a snapshot of the same size and rule set."""
         check(lib().se_world_load(self._h, os.fspath(path).encode()))
 
+    def set_tile(self, tile_w: int, tile_h: int, k: int) -> None:
+        """Use the compiled tile variant tile_w x tile_h with up to k frames per launch (an
+        override of the autotuner)."""
+        check(lib().se_world_set_tile(self._h, int(tile_w), int(tile_h), int(k)))
+
+    def tile(self):
+        """(tile_w, tile_h, k) of the variant multi-frame launches use."""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().se_world_get_tile(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
     def autotune(self, reps: int = 3) -> int:
         """Pick the fastest tile shape / frames per launch for this world (state unchanged);
         returns the chosen frames per launch."""
@@ -245,11 +256,17 @@ def snapshot_info(path: str) -> dict:
 
 
 def grid_digest(grid: np.ndarray) -> int:
-    """Host computation of Simulation.digest() for a (H, W) uint32 grid."""
-    g = np.ascontiguousarray(grid, dtype=np.uint32).ravel().astype(np.uint64)
-    z = (np.arange(g.size, dtype=np.uint64) << np.uint64(32)) | g
-    with np.errstate(over="ignore"):
-        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-        z = z ^ (z >> np.uint64(31))
-    return int(z.sum(dtype=np.uint64))
+    """Host computation of Simulation.digest() for a (H, W) uint32 grid (in slices of 2^24
+    cells, so a 2^28-cell grid needs no more than a few hundred MB of temporaries)."""
+    flat = np.ascontiguousarray(grid, dtype=np.uint32).ravel()
+    total = np.uint64(0)
+    step = 1 << 24
+    for s in range(0, flat.size, step):
+        g = flat[s:s + step].astype(np.uint64)
+        z = (np.arange(s, s + g.size, dtype=np.uint64) << np.uint64(32)) | g
+        with np.errstate(over="ignore"):
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            z = z ^ (z >> np.uint64(31))
+            total = total + z.sum(dtype=np.uint64)
+    return int(total)

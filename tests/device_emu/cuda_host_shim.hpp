@@ -12,6 +12,7 @@
 #define __device__
 #define __host__
 #define __global__
+#define __grid_constant__
 #define __forceinline__ inline
 #define __launch_bounds__(...)
 #define __shared__
@@ -64,7 +65,10 @@ inline unsigned __byte_perm(unsigned x, unsigned y, unsigned s) {
 inline unsigned __ballot_sync(unsigned, bool p) { return p ? 1u : 0u; }
 template <class T>
 inline T __shfl_sync(unsigned, T v, int) { return v; }
+template <class T>
+inline T __shfl_up_sync(unsigned, T v, unsigned) { return v; }  // lane 0: its own value
 inline int __popc(unsigned v) { return __builtin_popcount(v); }
+inline int __ffs(unsigned v) { return __builtin_ffs((int)v); }
 inline unsigned atomicOr(unsigned* p, unsigned v) {
   const unsigned old = *p;
   *p = old | v;

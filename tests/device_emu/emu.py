@@ -79,6 +79,18 @@ extern "C" void emu_tile_##TW##x##TH##_k##K(const uint32_t* src, uint32_t* dst, 
     } \
 }
 @TILES@
+#define EMU_TILE_EDIT(TW, TH, K) \
+extern "C" void emu_tile_edit_##TW##x##TH##_k##K(const uint32_t* src, uint32_t* dst, int W, int H, int f0, int k, \
+                                                int ya, int yb, const void* edits, int nedits) { \
+  blockDim.x = 1; threadIdx.x = 0; \
+  for (unsigned by = 0; by < (unsigned)((yb - ya + TH - 1) / TH); ++by) \
+    for (unsigned bx = 0; bx < (unsigned)((W + TW - 1) / TW); ++bx) { \
+      blockIdx.x = bx; blockIdx.y = by; \
+      se_tile_impl<TW, TH, K, 1>(src, dst, W, H, f0, k, g_lut, ya, yb, \
+                                 reinterpret_cast<const SeEditParams*>(edits), nedits); \
+    } \
+}
+@TILE_EDITS@
 #define EMU_MTILE(TW, TH, K) \
 extern "C" void emu_mtile_##TW##x##TH##_k##K(const SeWorldDesc* worlds, const SeTileJob* jobs, int njobs, \
                                              int pass, int done, int k) { \
@@ -130,9 +142,11 @@ class Emu:
         if "#define SE_CHECKED" not in src:  # every emulated launch runs the index checks
             src = "#define SE_CHECKED 1\n" + src
         tiles = "\n".join(f"EMU_TILE({a}, {b}, {c})" for a, b, c in VARIANTS)
+        tile_edits = "\n".join(f"EMU_TILE_EDIT({a}, {b}, {c})" for a, b, c in VARIANTS)
         mtiles = "\n".join(f"EMU_MTILE({a}, {b}, {c})" for a, b, c in VARIANTS)
         code = ('#include "cuda_host_shim.hpp"\n' + src +
-                DRIVER.replace("@TILES@", tiles).replace("@MTILES@", mtiles))
+                DRIVER.replace("@TILES@", tiles).replace("@TILE_EDITS@", tile_edits)
+                .replace("@MTILES@", mtiles))
         with open(os.path.join(HERE, "cuda_host_shim.hpp")) as f:
             shim = f.read()
         key = hashlib.sha256((code + shim).encode()).hexdigest()[:16]
@@ -229,9 +243,23 @@ class Emu:
         self._checked()
         return [o[1] for o in outs]
 
-    def edit(self, grid: np.ndarray, mods) -> None:
-        """The edit pass in place; host-side preparation as in runtime/engine.cpp."""
-        H, W = grid.shape
+    def tiles_edit(self, src: np.ndarray, f0: int, k: int, mods, variant=None) -> np.ndarray:
+        """k frames with one launch of the tile kernel's edit variant: the first frame's edit
+        pass (``mods``) inside the launch."""
+        if variant is None:
+            variant = min((v for v in VARIANTS if v[2] >= k), key=lambda v: v[2])
+        fn = getattr(self.lib, "emu_tile_edit_%dx%d_k%d" % variant)
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 6 + [ctypes.c_void_p, ctypes.c_int]
+        H, W = src.shape
+        buf, nlive, _ = self.edit_params(W, H, mods)
+        dst = np.zeros_like(src)
+        fn(src.ctypes.data, dst.ctypes.data, W, H, f0, k, 0, H, buf.ctypes.data, nlive)
+        self._checked()
+        return dst
+
+    def edit_params(self, W: int, H: int, mods):
+        """The SeEditParams block (as int32 words), the live mod count and the box cells,
+        prepared as runtime/engine.cpp's fill_edit_params does."""
         buf = np.zeros(14352 // 4, dtype=np.int32)
         m = buf[:2048].reshape(256, 8)
         box = buf[2048:3072].reshape(256, 4)
@@ -253,9 +281,17 @@ class Emu:
             if x1 >= x0 and y1 >= y0:
                 box[i] = (x0, y0, x1, y1)
                 total += (x1 - x0 + 1) * (y1 - y0 + 1)
+            else:
+                box[i] = (0, 0, -1, -1)
         start[len(live)] = total
+        return buf, len(live), total
+
+    def edit(self, grid: np.ndarray, mods) -> None:
+        """The edit pass in place; host-side preparation as in runtime/engine.cpp."""
+        H, W = grid.shape
+        buf, nlive, total = self.edit_params(W, H, mods)
         if total:
             self.lib.emu_edit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_longlong, ctypes.c_void_p]
-            self.lib.emu_edit(grid.ctypes.data, W, H, len(live), total, buf.ctypes.data)
+            self.lib.emu_edit(grid.ctypes.data, W, H, nlive, total, buf.ctypes.data)
             self._checked()

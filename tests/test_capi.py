@@ -50,3 +50,20 @@ def test_modification_record_layout():
     assert SeModification.mod_shape.offset == 8
     assert SeModification.mod_size.offset == 12
     assert SeModification.mod_matID.offset == 16
+
+
+def test_noalloc_histogram_rejects_bad_arguments_without_a_gpu(built_lib):
+    """se_grid_histogram_noalloc checks its arguments before any CUDA call: a null device
+    pointer, a null host pointer, and nbins outside [1, 257] are SE_ERR_INVALID_ARGUMENT
+    with a message."""
+    import ctypes
+    import numpy as np
+    from sandengine_gb300._lib import lib
+    L = lib()
+    out = np.zeros(8, dtype=np.uint64)
+    fake = ctypes.c_void_p(0x1000)  # never dereferenced: the call fails before any CUDA work
+    for dev, host, nbins in ((None, out.ctypes.data, 4), (fake, None, 4), (fake, out.ctypes.data, 0),
+                             (fake, out.ctypes.data, -3), (fake, out.ctypes.data, 258)):
+        rc = L.se_grid_histogram_noalloc(dev, 16, nbins, host, None)
+        assert rc == 1, (dev, host, nbins)
+        assert L.se_last_error()

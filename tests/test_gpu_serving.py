@@ -132,3 +132,61 @@ def test_cancelled_requests_are_skipped(se, ports, rulesets, plain):
     with pytest.raises(se.SandengineError):
         srv.latency_ms(rids[1])  # cancelled
     assert srv.latency_ms(rids[0]) >= 0
+
+
+@pytest.mark.parametrize("plain,budget", [(False, 256 << 20), (True, 256 << 20), (False, 6 << 20)])
+def test_live_loop_requests_from_another_thread(se, ports, rulesets, plain, budget):
+    """The live loop: requests submitted from a second thread while the loop runs (and while
+    earlier requests are on the GPU) are admitted and served; each session's result equals
+    the oracle's, as served alone; a request withdrawn before it starts is skipped; wait()
+    and poll() report completion.  With a 6 MB budget sessions are evicted to host memory
+    and restored while the loop runs."""
+    import threading
+    from sandengine_gb300.serving import Server
+    rs = se.parse_string(rulesets["twelve_materials"])
+    sessions, reqs = _workload()
+    srv = Server(rs, budget)
+    for (w, h, g, f) in sessions:
+        srv.open_session(w, h, g, f)
+    srv.start(plain=plain)
+    ids, cancelled = [None] * len(reqs), set()
+    # a long request ahead of the one to cancel keeps the latter queued behind it
+    srv.submit(3, 300, [], 0.0)
+    victim = srv.submit(3, 17, [], 0.0)
+    try:
+        srv.cancel(victim)
+        cancelled.add(victim)
+    except se.SandengineError:
+        pass  # it had started already: then it is served like any other request
+
+    def client(lo, hi):
+        for i in range(lo, hi):
+            s, nf, mods, _ = reqs[i]
+            ids[i] = srv.submit(s, nf, [se.SimModification((m[0], m[1]), m[2], m[3], m[4]) for m in mods])
+
+    # one thread submits the first half at once; this one the rest, after the loop is busy
+    t = threading.Thread(target=client, args=(0, len(reqs) // 2))
+    t.start()
+    t.join()
+    client(len(reqs) // 2, len(reqs))
+    lat = [srv.wait(r, 60000.0) for r in ids]
+    assert all(x >= 0 for x in lat)
+    assert srv.poll(ids[-1]) is not None
+    if cancelled:
+        with pytest.raises(se.SandengineError) as e:
+            srv.wait(victim, 0.0)
+        assert e.value.kind == "Cancelled"
+    srv.stop()
+    # the oracle: session 3 first advanced 300 frames (and 17 more when not cancelled)
+    extra = [(3, 300, [], 0.0)] + ([] if cancelled else [(3, 17, [], 0.0)])
+    order = []
+    for i in range(len(sessions)):
+        order += [r for r in extra if r[0] == i] + [r for r in reqs if r[0] == i]
+    want = _oracle(ports, sessions, order)
+    for i, (g, f) in enumerate(want):
+        assert np.array_equal(srv.grid(i), g), f"session {i}: live result differs from the oracle"
+        assert srv.frame(i) == f
+    st = srv.stats()
+    assert st["requests"] == len(reqs) + 2 - len(cancelled)
+    if budget < (7 << 20):
+        assert st["evictions"] > 0 and st["restores"] > 0, st

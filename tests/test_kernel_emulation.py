@@ -88,6 +88,28 @@ def test_edit_pass_matches_port(emus, ports, name):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("name", ["reference", "twelve_materials"])
+@pytest.mark.parametrize("variant", [(128, 64, 1), (128, 64, 8), (256, 128, 8), (64, 64, 4), (128, 128, 16)])
+def test_edits_inside_the_fused_launch_match_port(emus, ports, name, variant):
+    """The edit variant of the tile kernel: k frames in one launch whose first frame carries
+    the edit pass (applied in shared memory after that frame's block update, to halo cells
+    too), against the port's frame-then-edits.  Mods include circles and squares reaching
+    past the world, size 0 ending the list, an unknown material (NULL: no edit) over an
+    earlier hit, and WALL."""
+    w, h = 300, 200
+    E, P = emus[name], ports[name]
+    g = _world(name, w, h, 4)
+    mods = wl.circle_edits(w, h, 9, 0, 12, [0, 3, 200, 14]) + [
+        (5, 150, 1, 9, 5), (299, 0, 0, 30, 2), (150, 100, 1, 40, 3), (160, 100, 0, 12, 250),
+        (-4, 199, 1, 7, 4), (10, 10, 0, 0, 3), (1, 1, 1, 5, 4)]
+    k = variant[2]
+    for f in (10, 11, 12, 13):
+        want = g.copy()
+        P.run(want, f - 1, k, mods)
+        got = E.tiles_edit(g, f, k, mods, variant)
+        assert np.array_equal(got, want), f"frame {f}: {int(np.count_nonzero(got != want))} cells differ"
+
+
 @pytest.mark.parametrize("name", ["four_materials", "twelve_materials"])
 def test_static_key_bitset(se, rulesets, name):
     """Bit `key` of se_build_static's bitset is set exactly when every table entry of that

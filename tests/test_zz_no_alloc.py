@@ -2,9 +2,9 @@
 
 Callers such as a frame loop with all GPU memory sized up front, or a server whose HBM
 budget is fully committed, cannot call cudaMalloc when they need the counts; this entry
-point counts into a fixed static device array instead.  Its results must equal those of
-se_world_histogram (which counts into memory the world allocated) exactly, call after
-call, even though every call reuses the same array.  This file is collected last so that
+point counts into a fixed static device array instead.  Its results must equal a count of
+the grid read back to the host (and se_world_histogram's, which counts into memory the
+world allocated) exactly, call after call, even though every call reuses the same array.  This file is collected last so that
 a failure here does not stop the other tests of a run that stops at the first failure.
 """
 import ctypes
@@ -35,10 +35,12 @@ def test_noalloc_histogram_matches_world_histogram_twice(se, rulesets):
     sim.params.frame = 1
     nbins = rs.num_materials + 1
     for call in range(2):
-        want = sim.histogram(nbins)
+        grid = sim.grid  # read back to the host: the independent count
+        want = np.bincount(np.minimum(grid.ravel(), nbins - 1), minlength=nbins).astype(np.uint64)
         rc, got = _noalloc(L, sim.device_grid_ptr(), w * h, nbins, sim.stream)
         assert rc == 0, L.se_last_error()
         assert np.array_equal(got, want), f"call {call}: {got} != {want}"
+        assert np.array_equal(got, sim.histogram(nbins))  # and the allocating entry point agrees
         assert int(got.sum()) == w * h
         sim.run_frames(9)  # a different grid for the second call
 
