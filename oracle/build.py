@@ -6,9 +6,9 @@
 * ``Ref(yaml_text)``: the reference's own shaders/compute/falling_sand.glsl, flattened
   with the reference's include rule from the reference tree, rewritten by glsl2cpp and
   driven by oracle/ref_driver.cpp -> ``oracle/_ref/<hash>/ref.so``.  The translation step
-  reads the reference checkout (``SANDENGINE_REF`` or /root/reference) and writes the
-  generated source into oracle/_ref/; where no checkout exists but that generated source
-  does, it is compiled from there.
+  reads the reference checkout named by the ``SANDENGINE_REF`` environment variable and
+  writes the generated source into oracle/_ref/; where no checkout is named but that
+  generated source exists, it is compiled from there.
 
 Compiler flags: ``-O2 -ffp-contract=off`` (no FMA contraction, no fast-math) so binary32
 arithmetic matches the fixed IEEE semantics; OpenMP for the multi-core CPU baseline.
@@ -26,7 +26,7 @@ from typing import Optional
 import numpy as np
 
 from . import frontend as fe
-from .glsl2cpp import glsl_to_cpp
+from .glsl2cpp import fragment_to_cpp, glsl_to_cpp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
@@ -36,8 +36,9 @@ CXXFLAGS = ["-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fope
 
 
 def reference_root() -> Optional[str]:
-    r = os.environ.get("SANDENGINE_REF", "/root/reference")
-    return r if os.path.isdir(os.path.join(r, "shaders", "compute")) else None
+    """The reference checkout named by SANDENGINE_REF (None when unset or not a checkout)."""
+    r = os.environ.get("SANDENGINE_REF")
+    return r if r and os.path.isdir(os.path.join(r, "shaders", "compute")) else None
 
 
 def _digest(*parts: str) -> str:
@@ -120,6 +121,25 @@ def build_ref(yaml_text: str) -> str:
     return so
 
 
+def build_ref_frag() -> str:
+    """The reference's shaders/fragment140.glsl (fragment_to_cpp) driven by
+    oracle/frag_driver.cpp -> ``oracle/_ref/frag_<hash>/ref_frag.so``."""
+    srcs = [_read(os.path.join(HERE, f)) for f in ("frag_driver.cpp", "glsl_shim.hpp", "glsl2cpp.py")]
+    ref = reference_root()
+    d = os.path.join(REF_OUT, "frag_" + _digest(*srcs))
+    inc = os.path.join(d, "ref_frag.inc")
+    so = os.path.join(d, "ref_frag.so")
+    if os.path.exists(so):
+        return so
+    os.makedirs(d, exist_ok=True)
+    if ref is not None:
+        _write_if_changed(inc, fragment_to_cpp(_read(os.path.join(ref, "shaders", "fragment140.glsl"))))
+    elif not os.path.exists(inc):
+        raise FileNotFoundError("no reference checkout and no generated reference source")
+    _compile([os.path.join(HERE, "frag_driver.cpp")], so, [d, HERE])
+    return so
+
+
 MOD_DTYPE = np.dtype([("px", "<i4"), ("py", "<i4"), ("shape", "<i4"), ("size", "<i4"),
                       ("mat", "<i4"), ("pad", "<i4", (3,))])
 
@@ -142,6 +162,7 @@ class Port:
         self.lib.port_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         self.lib.port_hash43.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        self.lib.port_sin.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         self.lib.port_color.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         self.lib.port_light.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int]
         self.lib.port_mip_level.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
@@ -207,6 +228,13 @@ class Port:
         self.lib.port_run(grid.ctypes.data, grid.shape[1], grid.shape[0], frame0, nframes,
                           m.ctypes.data if len(m) else None, len(m), nthreads)
 
+    def sin(self, x: np.ndarray) -> np.ndarray:
+        """sin of binary32 arguments as the oracle (and the GPU colour pass) evaluates it."""
+        a = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.empty_like(a)
+        self.lib.port_sin(a.ctypes.data, out.ctypes.data, a.size)
+        return out
+
     def hash43(self, x: int, y: int, frame: int) -> np.ndarray:
         out = np.zeros(4, dtype=np.float32)
         self.lib.port_hash43(x, y, frame, out.ctypes.data)
@@ -259,3 +287,28 @@ class Ref:
         if light is not None:
             light[...] = lout
         return tex_out[..., 0].astype(np.int64).astype(np.uint32)
+
+
+class RefFrag:
+    """The reference's fragment shader (the composite of colour, light and background), run
+    on the CPU one pixel at a time with the samplers oracle/frag_driver.cpp fixes."""
+
+    def __init__(self):
+        self.lib = ctypes.CDLL(build_ref_frag())
+        self.lib.ref_frag_composite.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] + [ctypes.c_void_p] * 2 + \
+            [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+
+    def composite(self, levels, light=None, background=None) -> np.ndarray:
+        """levels: the colour field's pyramid, level 0 first (Port.mips); light: (H, W, 4)
+        float32 or None; background: (bh, bw, 4) float32 or None.  Returns (H, W, 4)."""
+        levels = [np.ascontiguousarray(lv, dtype=np.float32) for lv in levels]
+        ptrs = (ctypes.c_void_p * len(levels))(*[lv.ctypes.data for lv in levels])
+        lw = (ctypes.c_int * len(levels))(*[lv.shape[1] for lv in levels])
+        lh = (ctypes.c_int * len(levels))(*[lv.shape[0] for lv in levels])
+        li = None if light is None else np.ascontiguousarray(light, dtype=np.float32)
+        bg = None if background is None else np.ascontiguousarray(background, dtype=np.float32)
+        out = np.empty(levels[0].shape, dtype=np.float32)
+        self.lib.ref_frag_composite(ptrs, lw, lh, len(levels), None if li is None else li.ctypes.data,
+                                    None if bg is None else bg.ctypes.data, 0 if bg is None else bg.shape[1],
+                                    0 if bg is None else bg.shape[0], out.ctypes.data)
+        return out

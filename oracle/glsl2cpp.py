@@ -15,6 +15,11 @@ shader computes:
 * ``void main()`` is renamed ``glsl_main()``;
 * struct ``Material``/``Cell``/``SimModification`` get a defaulted ``operator==`` (GLSL
   compares structs member-wise).
+
+``fragment_to_cpp`` applies, before those, the rewrites a fragment shader needs: the
+global ``in``/``out`` storage qualifiers are dropped (the driver sets the inputs and reads
+the outputs as globals), and assignments to the ``.rgb`` swizzle (``v.rgb = e;``,
+``v.rgb *= e;``) become ``v.set_rgb(e);`` / ``v.set_rgb(v.rgb * (e));``.
 """
 from __future__ import annotations
 
@@ -46,3 +51,10 @@ def glsl_to_cpp(src: str) -> str:
         s = re.sub(r"(struct\s+" + name + r"\s*\{)",
                    r"\1 bool operator==(const " + name + r"&) const = default;", s)
     return s
+
+
+def fragment_to_cpp(src: str) -> str:
+    s = re.sub(r"^(\s*)(?:in|out)\s+(?=\w+\s+\w+\s*;)", r"\1", src, flags=re.M)
+    s = re.sub(r"\b(\w+)\.rgb\s*\*=\s*([^;]+);", r"\1.set_rgb(\1.rgb * (\2));", s)
+    s = re.sub(r"\b(\w+)\.rgb\s*=(?!=)\s*([^;]+);", r"\1.set_rgb(\2);", s)
+    return glsl_to_cpp(s)

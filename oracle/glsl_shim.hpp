@@ -51,6 +51,7 @@ struct vec4 {
   vec4(const ivec4& u);
   vec3 rgb() const { return vec3(x, y, z); }
   vec2 xy() const { return vec2(x, y); }
+  void set_rgb(const vec3& v) { x = v.x; y = v.y; z = v.z; }  // `v.rgb = e` (glsl2cpp)
 };
 
 struct ivec2 {
@@ -115,6 +116,8 @@ inline vec2 operator-(vec2 a) { return vec2(-a.x, -a.y); }
 inline vec2& operator+=(vec2& a, vec2 b) { a = a + b; return a; }
 inline vec2& operator*=(vec2& a, float b) { a = a * b; return a; }
 inline vec4& operator+=(vec4& a, vec4 b) { a = a + b; return a; }
+inline vec4& operator*=(vec4& a, vec4 b) { a = a * b; return a; }
+inline vec3& operator+=(vec3& a, vec3 b) { a = a + b; return a; }
 inline vec4& operator/=(vec4& a, float b) { a = a / b; return a; }
 inline bool operator==(vec3 a, vec3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 inline bool operator!=(vec3 a, vec3 b) { return !(a == b); }
@@ -157,7 +160,39 @@ inline float floor(float x) { return __builtin_floorf(x); }
 inline vec2 floor(vec2 v) { return vec2(floor(v.x), floor(v.y)); }
 inline float fract(float x) { return x - floor(x); }
 inline vec2 fract(vec2 v) { return vec2(fract(v.x), fract(v.y)); }
-inline float sin(float x) { return __builtin_sinf(x); }
+// GLSL leaves sin's precision to the driver.  The oracle fixes it to this evaluation (the
+// one the GPU colour pass makes): binary64 with Cody and Waite's argument reduction (W. J.
+// Cody, W. Waite, Software Manual for the Elementary Functions, 1980; pi/2 as three 21-bit
+// parts and a binary64 tail) and the Taylor series of sin (to r^17) or cos (to r^18) on
+// |r| <= pi/4, rounded once to binary32: within 1 ulp of sin(x).  Compiled without
+// contraction, so every operation rounds as the GPU's explicit intrinsics do.
+inline float se_sin(float xf) {
+  const double x = (double)xf;
+  if (!(__builtin_fabs(x) < 0x1p52)) return (float)(x - x);
+  if (__builtin_fabs(x) < 0x1p-12) return xf;  // sin(x) rounds to x (keeps the sign of zero)
+  const double k = __builtin_floor(x * 0x1.45f306dc9c883p-1 + 0.5);
+  double r = x - k * 0x1.921fb0p+0;
+  r = r - k * 0x1.5110bp-22;
+  r = r - k * 0x1.18469p-44;
+  r = r - k * 0x1.13198a2e03707p-65;
+  const double r2 = r * r;
+  const double ps_c[8] = {0x1.952c77030ad4ap-49, -0x1.ae7f3e733b81fp-41, 0x1.6124613a86d09p-33,
+                          -0x1.ae64567f544e4p-26, 0x1.71de3a556c734p-19, -0x1.a01a01a01a01ap-13,
+                          0x1.1111111111111p-7, -0x1.5555555555555p-3};  // (-1)^n / (2n+1)!, n = 8..1
+  const double pc_c[9] = {-0x1.6827863b97d97p-53, 0x1.ae7f3e733b81fp-45, -0x1.93974a8c07c9dp-37,
+                          0x1.1eed8eff8d898p-29, -0x1.27e4fb7789f5cp-22, 0x1.a01a01a01a01ap-16,
+                          -0x1.6c16c16c16c17p-10, 0x1.5555555555555p-5, -0.5};  // (-1)^n / (2n)!, n = 9..1
+  double ps = ps_c[0];
+  for (int i = 1; i < 8; ++i) ps = ps * r2 + ps_c[i];
+  const double sn = r + (r * r2) * ps;
+  double pc = pc_c[0];
+  for (int i = 1; i < 9; ++i) pc = pc * r2 + pc_c[i];
+  const double cs = 1.0 + r2 * pc;
+  const double q = k - 4.0 * __builtin_floor(k * 0.25);  // k mod 4, exact
+  const double v = q == 0.0 ? sn : q == 1.0 ? cs : q == 2.0 ? -sn : -cs;
+  return (float)v;
+}
+inline float sin(float x) { return se_sin(x); }
 inline vec2 sin(vec2 v) { return vec2(sin(v.x), sin(v.y)); }
 inline float cos(float x) { return __builtin_cosf(x); }
 inline float tan(float x) { return __builtin_tanf(x); }
@@ -176,6 +211,20 @@ inline float dot(vec4 a, vec4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.
 inline float length(vec2 v) { return sqrt(dot(v, v)); }
 inline float distance(vec2 a, vec2 b) { return length(a - b); }
 inline vec3 mix(vec3 x, vec3 y, float a) { return x * (1.0f - a) + y * a; }
+inline vec4 mix(vec4 x, vec4 y, float a) { return x * (1.0f - a) + y * a; }
+inline float exp(float x) { return __builtin_expf(x); }
+inline float log2(float x) { return __builtin_log2f(x); }
+inline vec2 clamp(vec2 x, vec2 lo, vec2 hi) { return vec2(clamp(x.x, lo.x, hi.x), clamp(x.y, lo.y, hi.y)); }
+inline vec3 clamp(vec3 x, vec3 lo, vec3 hi) {
+  return vec3(clamp(x.x, lo.x, hi.x), clamp(x.y, lo.y, hi.y), clamp(x.z, lo.z, hi.z));
+}
+inline float smoothstep(float e0, float e1, float x) {  // the GLSL specification's definition
+  const float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+inline vec2 smoothstep(vec2 e0, vec2 e1, vec2 x) {
+  return vec2(smoothstep(e0.x, e1.x, x.x), smoothstep(e0.y, e1.y, x.y));
+}
 
 // ---- fixed-size arrays with GLSL's .length() ---------------------------------------------
 template <class T, int N>
@@ -191,10 +240,13 @@ struct garr {
 };
 
 // ---- CPU textures (RGBA32F) -----------------------------------------------------------------
+// The fragment stage's filtered, mipmapped samplers are oracle/frag_driver.cpp's.
+#ifndef SE_GLSL_FRAGMENT
 struct sampler2D {
   const float* data = nullptr;  // W*H*4 floats, row-major
   int w = 0, h = 0;
 };
+#endif
 struct image2D {
   float* data = nullptr;
   int w = 0, h = 0;
@@ -203,12 +255,14 @@ struct uimage2D {
   uint* data = nullptr;
   int w = 0, h = 0;
 };
+#ifndef SE_GLSL_FRAGMENT
 inline vec4 texelFetch(const sampler2D& s, ivec2 p, int) {
   // Out-of-range fetches return 0 (robust buffer access); the shader guards its fetches.
   if (p.x < 0 || p.y < 0 || p.x >= s.w || p.y >= s.h || !s.data) return vec4(0.0f);
   const float* t = s.data + 4 * ((long)p.y * s.w + p.x);
   return vec4(t[0], t[1], t[2], t[3]);
 }
+#endif
 inline void imageStore(image2D& im, ivec2 p, vec4 v) {
   if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h || !im.data) return;
   float* t = im.data + 4 * ((long)p.y * im.w + p.x);

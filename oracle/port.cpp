@@ -269,6 +269,13 @@ SE_EXPORT void port_run(uint32_t* grid, int W, int H, int frame0, int nframes, c
 }  // extern "C"
 namespace {
 
+extern "C" {
+// sin as the oracle evaluates it (glsl_shim.hpp se_sin), for n arguments.
+SE_EXPORT void port_sin(const float* in, float* out, int n) {
+  for (int i = 0; i < n; ++i) out[i] = se_sin(in[i]);
+}
+}  // extern "C"
+
 // math.glsl:40-44 old_hash2, one component: -1 + 2 * fract(sin(q) * 43758.5453123).
 inline float grad_component(float q) {
   const float v = sin(q) * 43758.5453123f;

@@ -2,10 +2,10 @@
 // shaders/compute/operations.glsl:99-169 with math.glsl:40-44,82-106.
 //
 // Every float operation is an explicit round-to-nearest intrinsic in the shader's order, so
-// nothing is contracted into FMAs: the light pass equals a strict-IEEE CPU evaluation bit
-// for bit.  The colour's noise calls sinf (CUDA's, not a fast approximation); the
-// reference's GLSL sin is driver-defined, so colours agree with a CPU evaluation only
-// within the error that a last-place difference of sin leaves after the gradient hash.
+// nothing is contracted into FMAs: the light pass and the colour equal a strict-IEEE CPU
+// evaluation bit for bit.  GLSL leaves the precision of sin to the driver; the colour's
+// noise fixes it to se_sin (below), which the CPU oracle evaluates with the same binary64
+// operations.
 #include "render.hpp"
 
 #include <algorithm>
@@ -21,9 +21,57 @@ __device__ __forceinline__ float gmax(float a, float b) { return a < b ? b : a; 
 __device__ __forceinline__ float gmin(float a, float b) { return b < a ? b : a; }
 __device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
 
+// sin of a binary32 argument: evaluated in binary64 and rounded once to binary32.
+// Argument reduction by Cody and Waite's method (W. J. Cody, W. Waite, Software Manual for
+// the Elementary Functions, 1980): k = the nearest integer to x * 2/pi, r = x - k * pi/2
+// with pi/2 split into three 21-bit parts (k * part is exact for |k| < 2^32) and a
+// binary64 tail, so r carries about 2^-100 absolute error for |x| < 2^30.  Then the Taylor
+// series of sin (to r^17) or cos (to r^18) on |r| <= pi/4 (truncation below 1e-19),
+// chosen and signed by k mod 4.  The result is the correctly rounded sinf(x) except when
+// the binary64 value lies within about 1e-16 (relative) of a rounding boundary; it is
+// within 1 ulp of sin(x), inside CUDA's documented 2-ulp bound for sinf.  Every operation
+// is an explicit round-to-nearest binary64 intrinsic (no contraction), so the CPU oracle's
+// restatement gives the same bits.  |x| < 2^-12 gives x (the correctly rounded value);
+// |x| >= 2^52 (never met: the noise's arguments stay below 2^30) gives x - x (NaN for
+// infinities and NaN, else 0).
+__device__ __forceinline__ float se_sin(float xf) {
+  const double x = (double)xf;
+  if (!(fabs(x) < 0x1p52)) return (float)__dsub_rn(x, x);
+  if (fabs(x) < 0x1p-12) return xf;  // sin(x) rounds to x (keeps the sign of zero)
+  const double k = floor(__dadd_rn(__dmul_rn(x, 0x1.45f306dc9c883p-1), 0.5));
+  double r = __dsub_rn(x, __dmul_rn(k, 0x1.921fb0p+0));
+  r = __dsub_rn(r, __dmul_rn(k, 0x1.5110bp-22));
+  r = __dsub_rn(r, __dmul_rn(k, 0x1.18469p-44));
+  r = __dsub_rn(r, __dmul_rn(k, 0x1.13198a2e03707p-65));
+  const double r2 = __dmul_rn(r, r);
+  // Taylor coefficients (-1)^n / (2n+1)! and (-1)^n / (2n)!, rounded to binary64
+  double ps = 0x1.952c77030ad4ap-49;                       // 1/17!
+  ps = __dadd_rn(__dmul_rn(ps, r2), -0x1.ae7f3e733b81fp-41);  // -1/15!
+  ps = __dadd_rn(__dmul_rn(ps, r2), 0x1.6124613a86d09p-33);   // 1/13!
+  ps = __dadd_rn(__dmul_rn(ps, r2), -0x1.ae64567f544e4p-26);  // -1/11!
+  ps = __dadd_rn(__dmul_rn(ps, r2), 0x1.71de3a556c734p-19);   // 1/9!
+  ps = __dadd_rn(__dmul_rn(ps, r2), -0x1.a01a01a01a01ap-13);  // -1/7!
+  ps = __dadd_rn(__dmul_rn(ps, r2), 0x1.1111111111111p-7);    // 1/5!
+  ps = __dadd_rn(__dmul_rn(ps, r2), -0x1.5555555555555p-3);   // -1/3!
+  const double sn = __dadd_rn(r, __dmul_rn(__dmul_rn(r, r2), ps));
+  double pc = -0x1.6827863b97d97p-53;                      // -1/18!
+  pc = __dadd_rn(__dmul_rn(pc, r2), 0x1.ae7f3e733b81fp-45);   // 1/16!
+  pc = __dadd_rn(__dmul_rn(pc, r2), -0x1.93974a8c07c9dp-37);  // -1/14!
+  pc = __dadd_rn(__dmul_rn(pc, r2), 0x1.1eed8eff8d898p-29);   // 1/12!
+  pc = __dadd_rn(__dmul_rn(pc, r2), -0x1.27e4fb7789f5cp-22);  // -1/10!
+  pc = __dadd_rn(__dmul_rn(pc, r2), 0x1.a01a01a01a01ap-16);   // 1/8!
+  pc = __dadd_rn(__dmul_rn(pc, r2), -0x1.6c16c16c16c17p-10);  // -1/6!
+  pc = __dadd_rn(__dmul_rn(pc, r2), 0x1.5555555555555p-5);    // 1/4!
+  pc = __dadd_rn(__dmul_rn(pc, r2), -0.5);                    // -1/2!
+  const double cs = __dadd_rn(1.0, __dmul_rn(r2, pc));
+  const double q = __dsub_rn(k, __dmul_rn(4.0, floor(__dmul_rn(k, 0.25))));  // k mod 4, exact
+  const double v = q == 0.0 ? sn : q == 1.0 ? cs : q == 2.0 ? -sn : -cs;
+  return __double2float_rn(v);
+}
+
 // old_hash2 component: -1 + 2 * fract(sin(q) * 43758.5453123)
 __device__ __forceinline__ float grad_component(float q) {
-  const float v = fmul(sinf(q), 43758.5453123f);
+  const float v = fmul(se_sin(q), 43758.5453123f);
   return fadd(-1.0f, fmul(2.0f, fsub(v, floorf(v))));
 }
 __device__ __forceinline__ void grad(float qx, float qy, float& gx, float& gy) {

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import frontend as fe
-from oracle.build import Port, Ref, reference_root
+from oracle.build import Port, Ref, RefFrag, reference_root
 from sandengine_gb300.simulation import grid_digest
 from tests.conftest import GOLDEN
 from tests.golden.cases import CASES
@@ -19,6 +19,15 @@ from tests.golden.yaml_corpus import CORPUS
 def _gen_golden():
     with open(os.path.join(GOLDEN, "reference_gen.json")) as f:
         return json.load(f)
+
+
+def _ref(text):
+    """The reference shader compiled for the CPU: from the checkout SANDENGINE_REF names, or
+    from the translated source an earlier build left in oracle/_ref (skip if neither)."""
+    try:
+        return Ref(text)
+    except FileNotFoundError:
+        pytest.skip("no reference checkout (SANDENGINE_REF) and no translated reference source")
 
 
 def test_frontend_reproduces_reference_generated_glsl(rulesets):
@@ -31,7 +40,7 @@ def test_frontend_reproduces_reference_generated_glsl(rulesets):
         assert hashlib.sha256(data).hexdigest() == gold[name]["sha256"]
 
 
-@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout")
+@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout (SANDENGINE_REF)")
 def test_flattener_reproduces_reference_falling_sand():
     from oracle.build import reference_shader_text
     with open(os.path.join(GOLDEN, "reference_materials.yaml")) as f:
@@ -102,13 +111,12 @@ def test_port_matches_reference_digests(case):
         assert grid_digest(g) == int(gold[i]), f"frame {case.frame0 + 1 + i}"
 
 
-@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout")
 @pytest.mark.parametrize("name", ["reference", "four_materials", "twelve_materials"])
 def test_port_matches_reference_shader(rulesets, name):
     """Random worlds with unknown ids, WALL/NULL cells and overlapping edits of every
     kind (unknown material, size 0 terminator, negative position, squares)."""
     text = rulesets[name]
-    P, R = Port(text), Ref(text)
+    P, R = Port(text), _ref(text)
     rng = np.random.default_rng(7)
     for H, W in ((37, 50), (16, 16), (5, 9)):
         g = rng.integers(0, P.num_materials + 3, size=(H, W)).astype(np.uint32)
@@ -124,11 +132,10 @@ def test_port_matches_reference_shader(rulesets, name):
             assert np.array_equal(gp, gr), f"{name} {H}x{W} frame {f}"
 
 
-@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout")
 def test_port_edit_pass_extreme_mods(rulesets):
     """Mods far outside the grid, huge radii and positions whose difference wraps."""
     text = rulesets["four_materials"]
-    P, R = Port(text), Ref(text)
+    P, R = Port(text), _ref(text)
     g = np.zeros((20, 24), dtype=np.uint32)
     g[5:15, 5:15] = 3
     mods = [(-2**31 + 3, 4, 1, 2**31 - 1, 4), (12, 10, 0, 2**23, 5), (2**31 - 1, -2**31, 0, 7, 3),
@@ -140,7 +147,6 @@ def test_port_edit_pass_extreme_mods(rulesets):
         assert np.array_equal(gp, gr)
 
 
-@pytest.mark.skipif(reference_root() is None, reason="needs the reference checkout")
 @pytest.mark.parametrize("name", ["reference", "twelve_materials"])
 def test_port_color_and_light_match_reference_shader(rulesets, name):
     """The port's colour (material colour minus 3-octave noise) and light propagation equal
@@ -148,7 +154,7 @@ def test_port_color_and_light_match_reference_shader(rulesets, name):
     frame (the light field carried over), with edits, emitting materials (the twelve set
     has two), the frame-1 clear and worlds wider than the noise period."""
     text = rulesets[name]
-    P, R = Port(text), Ref(text)
+    P, R = Port(text), _ref(text)
     rng = np.random.default_rng(11)
     for H, W, f0 in ((40, 300, 2), (17, 23, 0)):
         g = rng.integers(0, P.num_materials + 2, size=(H, W)).astype(np.uint32)
@@ -199,3 +205,53 @@ def test_port_composite_known_answers(rulesets):
     assert lv[1].shape == (16, 16, 4)
     assert np.allclose(lv[1], bg.reshape(16, 2, 16, 2, 4).mean(axis=(1, 3)), rtol=1e-6, atol=1e-7)
     assert lv[-1].shape == (1, 1, 4)
+
+
+def test_oracle_sin_is_sin_rounded_once(ports):
+    """GLSL leaves sin's precision to the driver; the oracle (and the GPU colour pass) fix it
+    to binary64 evaluation (Cody-Waite reduction, Taylor series) rounded once to binary32.
+    Over magnitudes 2^-20 .. 2^30 (the colour noise's arguments stay below 2^30) it equals
+    the binary64 sin rounded to binary32 on every sampled argument, and it is within 1 ulp
+    of that by construction."""
+    P = ports["twelve_materials"]
+    rng = np.random.default_rng(1)
+    mag = 2.0 ** rng.uniform(-20, 30, 400_000)
+    x = (mag * rng.choice([-1, 1], mag.size)).astype(np.float32)
+    ix, iy = np.meshgrid(np.arange(-300, 300, dtype=np.float32), np.arange(0, 200, dtype=np.float32))
+    q = (ix * np.float32(127.1) + iy * np.float32(311.7)).ravel()  # old_hash2's arguments
+    x = np.concatenate([x, q, np.float32([0.0, -0.0, 1e-30, np.pi / 2, np.pi, 1e9])])
+    ours = P.sin(x)
+    want = np.sin(x.astype(np.float64)).astype(np.float32)
+    ulp = np.abs(ours.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+    assert ulp.max() <= 1
+    assert np.count_nonzero(ulp) <= x.size // 100000
+    special = P.sin(np.float32([np.inf, -np.inf, np.nan, 2.0**60]))
+    assert np.isnan(special[:3]).all() and special[3] == 0.0
+
+
+def _ref_frag():
+    try:
+        return RefFrag()
+    except FileNotFoundError:
+        pytest.skip("no reference checkout (SANDENGINE_REF) and no translated reference source")
+
+
+@pytest.mark.parametrize("shape", [(64, 48), (333, 517), (7, 5), (1, 33), (2, 1)])
+def test_port_composite_matches_reference_fragment_shader(rulesets, shape):
+    """The composite's restatement (port_composite) equals the reference's own
+    shaders/fragment140.glsl, compiled for the CPU from its text and run per pixel with the
+    samplers the composite fixes (nearest magnification and LINEAR_MIPMAP_NEAREST for the
+    colour pyramid, bilinear light and background, mirrored repeat), bit for bit: with a
+    light field and a background image, with light alone, and with neither."""
+    W, H = shape
+    P, F = Port(rulesets["twelve_materials"]), _ref_frag()
+    rng = np.random.default_rng(W * 1000 + H)
+    g = rng.integers(0, P.num_materials + 2, size=(H, W)).astype(np.uint32)
+    g[rng.random((H, W)) < 0.4] = 0
+    col = P.color(g)
+    light = (rng.random((H, W, 4)) * 1.5).astype(np.float32)
+    bg = rng.random((211, 157, 4)).astype(np.float32)
+    for li, b in ((light, bg), (light, None), (None, None)):
+        want = P.composite(col, li, b)
+        got = F.composite(P.mips(col), li, b)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
