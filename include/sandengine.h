@@ -249,6 +249,10 @@ int se_grid_histogram_noalloc(const uint32_t* device_cells, uint64_t count, int 
 int se_world_set_timing(se_world* w, int enable);
 int se_world_read_timing(se_world* w, double* kernel_ms, long long* launches, long long* cell_frames,
                          long long* cells);
+/* The summed kernel time and the number of the tile launches since the last read that
+ * advanced exactly `frames` frames each (synchronizes; does not reset: se_world_read_timing
+ * does).  The roofline of one fusion depth, e.g. the k = 8 launches of 60-frame steps. */
+int se_world_peek_timing_frames(se_world* w, int frames, double* kernel_ms, long long* launches);
 /* The same for the light pass (pass = 1; algorithmic bytes 40 x cells: old and new id, old
  * and new RGBA32F light), the colour pass (pass = 2; 24 x cells: id, noise, RGBA32F) and the
  * composite (pass = 3; 48 x cells: colour, light, output; its pyramid is not timed). */

@@ -133,6 +133,8 @@ _SIGS = {
     "se_world_load": ([_P, ctypes.c_char_p], _I),
     "se_server_save_session": ([_P, _I, ctypes.c_char_p], _I),
     "se_server_open_session_from": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
+    "se_world_peek_timing_frames": ([_P, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)],
+                                    _I),
     "se_world_read_timing": ([_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                               ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)], _I),
 }

@@ -535,6 +535,13 @@ SE_API int se_world_read_timing(se_world* w, double* kernel_ms, long long* launc
   });
 }
 
+SE_API int se_world_peek_timing_frames(se_world* w, int frames, double* kernel_ms, long long* launches) {
+  return guard([&] {
+    if (!w || !kernel_ms || !launches) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    return ret(w->w->timing_peek_frames(frames, kernel_ms, launches));
+  });
+}
+
 SE_API int se_world_read_pass_timing(se_world* w, int pass, double* kernel_ms, long long* launches,
                                      long long* cells) {
   return guard([&] {

@@ -255,6 +255,23 @@ Status World::timing_begin(int pass, long long cells, int frames, Timed** out) {
   return Status::Ok();
 }
 
+Status World::timing_peek_frames(int frames, double* ms, long long* launches) {
+  SE_CUDA(cudaStreamSynchronize(stream));
+  double tot = 0;
+  long long n = 0;
+  const auto& set = timed[0];
+  for (size_t i = 0; i < timed_used[0]; ++i) {
+    if (set[i].frames != frames) continue;
+    float m = 0;
+    SE_CUDA(cudaEventElapsedTime(&m, set[i].a, set[i].b));
+    tot += m;
+    ++n;
+  }
+  *ms = tot;
+  *launches = n;
+  return Status::Ok();
+}
+
 Status World::timing_read(int pass, double* ms, long long* launches, long long* cell_frames, long long* cells) {
   if (pass < 0 || pass > 3)
     return {SE_ERR_INVALID_ARGUMENT, "pass must be 0 (tiles), 1 (light), 2 (colour) or 3 (composite)"};

@@ -106,6 +106,7 @@ struct World {
   size_t timed_used[4] = {0, 0, 0, 0};
   Status timing_begin(int pass, long long cells, int frames, Timed** out);
   Status timing_read(int pass, double* ms, long long* launches, long long* cell_frames, long long* cells);
+  Status timing_peek_frames(int frames, double* ms, long long* launches);  // tile launches of `frames` frames
   Status digest(unsigned long long* out);
   Status histogram(unsigned long long* counts, int nbins);
 

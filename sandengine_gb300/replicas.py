@@ -4,6 +4,10 @@ Worlds are independent, so a multi-GPU run is N replicas with no data-path colle
 each rank advances its own world(s); the only communication is a barrier around the timed
 region and a max/sum of the per-rank results.  Launched by torch.distributed.run (RANK,
 LOCAL_RANK, WORLD_SIZE, MASTER_ADDR/PORT from the environment).
+
+With NCCL each rank is pinned to its GPU through CUDA_VISIBLE_DEVICES before any CUDA
+call, so the library's kernels (its own CUDA runtime state) and torch both see that GPU as
+device 0.
 """
 from __future__ import annotations
 
@@ -17,10 +21,13 @@ class Replicas:
         self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = None
         if self.world_size > 1:
-            import torch.distributed as dist
             if backend == "nccl":
+                visible = [d for d in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if d.strip()]
+                os.environ["CUDA_VISIBLE_DEVICES"] = (visible[self.local_rank] if self.local_rank < len(visible)
+                                                      else str(self.local_rank))
                 import torch
-                torch.cuda.set_device(self.local_rank)
+                torch.cuda.set_device(0)
+            import torch.distributed as dist
             dist.init_process_group(backend=backend)
             self.pg = dist
 
@@ -32,7 +39,7 @@ class Replicas:
         if not self.pg:
             return value
         import torch
-        dev = f"cuda:{self.local_rank}" if self.pg.get_backend() == "nccl" else "cpu"
+        dev = "cuda:0" if self.pg.get_backend() == "nccl" else "cpu"
         t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
         self.pg.all_reduce(t, op=getattr(self.pg.ReduceOp, op))
         return float(t.item())

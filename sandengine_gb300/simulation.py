@@ -165,6 +165,13 @@ class Simulation:
         """Bracket every tile-kernel launch with CUDA events (see read_timing)."""
         check(lib().se_world_set_timing(self._h, 1 if enable else 0))
 
+    def peek_timing_frames(self, frames: int) -> dict:
+        """Kernel time and launches of the timed tile launches of exactly `frames` frames
+        since the last read_timing (synchronizes; does not reset)."""
+        ms, n = ctypes.c_double(), ctypes.c_longlong()
+        check(lib().se_world_peek_timing_frames(self._h, int(frames), ctypes.byref(ms), ctypes.byref(n)))
+        return {"kernel_ms": ms.value, "launches": n.value}
+
     def read_timing(self) -> dict:
         """Kernel time, launches, cell updates and cells read by tile launches since the
         last read (synchronizes)."""

@@ -114,3 +114,13 @@ def twelve_fill_spec(num_materials: int = 15):
 def world_16384(seed: int = 2, size: int = 16384) -> np.ndarray:
     """16384^2 (or ``size``^2), twelve materials, 64x64 patches (seed 2)."""
     return patch_fill(size, size, seed, *twelve_fill_spec())
+
+
+WORLD_EDITS_PER_ROUND = 32
+WORLD_FRAMES_PER_ROUND = 60
+
+
+def world_edits(size: int, round_idx: int, materials: Sequence[int] = (0, 3)):
+    """The edit round ``round_idx`` of the size^2 patch world: 32 circles (radius 8-64,
+    uniform positions, EMPTY or sand), applied on the first frame of every 60."""
+    return circle_edits(size, size, 2, round_idx, WORLD_EDITS_PER_ROUND, materials)
