@@ -1,8 +1,8 @@
 """Regenerates the golden fixtures in this folder from the reference checkout.
 
-Run in a container that has the reference tree (SANDENGINE_REF or /root/reference):
+Run with the reference checkout named by SANDENGINE_REF:
 
-    python tests/golden/make_golden.py
+    SANDENGINE_REF=<reference checkout> python tests/golden/make_golden.py
 
 Writes
   reference_materials.yaml   the reference's data/materials.yaml (the rule-set fixture whose
