@@ -79,6 +79,7 @@ def parse_args():
     ap.add_argument("--no-batched", action="store_true", help="world workloads: leave out the batched figures")
     ap.add_argument("--no-serving", action="store_true", help="world workloads: leave out the serving figures")
     ap.add_argument("--serve-requests", type=int, default=300, help="requests per arrival rate")
+    ap.add_argument("--serve-k", type=int, default=8, help="frames per batched serving iteration")
     ap.add_argument("--light", action="store_true",
                     help="world workloads: keep the light field (light pass after every frame, one-frame "
                          "launches) and composite the frame once per step")
@@ -319,6 +320,13 @@ def run_ours(args, rep):
     for r in range(args.warmup):
         one_step(r)
     sim.synchronize()
+    if not args.k and not args.tile:
+        # tune again on the warmed-up world: its state (half of the chunks dynamic) is the one
+        # the timed steps see, unlike the freshly filled world the first tuning saw
+        k = sim.autotune(3)
+        tile = sim.tile()
+        one_step(0)
+        sim.synchronize()
 
     sim.set_timing(True)
     sim.read_timing()
@@ -377,12 +385,19 @@ def run_ours(args, rep):
         "config": {"workload": f"{spec['name']}: {W}x{H} u32 cells, {spec['ruleset']} rule set, {spec['fill']}, "
                                f"{FRAMES_PER_STEP} frames per step, {EDITS_PER_STEP} circle edits on the first",
                    "frames_per_launch": k, "tile": f"{tile[0]}x{tile[1]}",
+                   "tuning": ("fixed by --k/--tile" if (args.k or args.tile) else
+                              "autotuned on the fresh world, then again after the warm-up steps "
+                              "(one more untimed step follows)"),
                    "l2": "inputs larger than L2 (1 GiB per buffer)" if W >= 8192
                    else "world fits in L2; no flush", "parallelism": f"replicas{rep.world_size}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "traffic_source": traffic_source,
-                     "kernel": f"se_tile (k={k})", "peak_source": peak_src,
+                     "kernel": f"se_tile_{tile[0]}x{tile[1]}_k{tile[2]} (up to {k} frames per launch)",
+                     "peak_source": peak_src,
+                     "bound_note": "issue-bound at k >= 2: the integer ALU pipe runs at 73% of its peak and DRAM "
+                                   "traffic equals the algorithmic bytes (profiles/tile_kernel_256x128_k8_world16384.md); "
+                                   "one_frame_launches gives the same kernel at one frame per launch, HBM-bound",
                      "algorithmic_bytes_per_launch": alg_bytes_per_launch,
                      "avg_launch_ms": avg_launch_s * 1e3, "launches": launches,
                      "k_launches": timing_k["launches"], "k_launch_avg_ms": k_launch_ms,
@@ -412,6 +427,20 @@ def run_ours(args, rep):
                                       "(colour render, pyramid, composite) per step")
     if e2e:
         out["e2e"] = e2e
+    if spec["name"] == "world16384" and not args.light and not args.k and not args.tile:
+        # the same kernel at one frame per launch, the memory-bound form: two 60-frame steps
+        sim.set_steps_per_launch(1)
+        sim.set_timing(True)
+        sim.read_timing()
+        for r in range(2):
+            sim.run_frames(FRAMES_PER_STEP, mods[r % len(mods)])
+        t1 = sim.read_timing()
+        sim.set_timing(False)
+        avg1 = t1["kernel_ms"] / max(t1["launches"], 1)
+        ach1 = 8.0 * W * H / (avg1 / 1e3) / 1e9
+        out["one_frame_launches"] = {"launches": t1["launches"], "avg_launch_ms": avg1, "achieved": ach1,
+                                     "peak": peak, "unit": "GB/s", "frac": ach1 / peak,
+                                     "cell_updates_per_s": float(W) * H / (avg1 / 1e3)}
     if rep.rank == 0 and rep.world_size == 1 and not args.no_cpu_baseline:
         rate, kind, cores, sample = cpu_rate(W, spec, args.cpu_seconds)
         out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
@@ -425,7 +454,7 @@ def run_ours(args, rep):
         if not args.no_batched:
             out["batched"] = measure_batch(rep, 4096, steps=20, warmup=3)
         if not args.no_serving:
-            out["serving"] = measure_serving(rep, args.serve_requests)
+            out["serving"] = measure_serving(rep, args.serve_requests, args.serve_k)
     return out
 
 
@@ -550,7 +579,7 @@ SERVE_BUDGET = 150 << 30
 SERVE_SMALL_BUDGET = 256 << 20
 
 
-def measure_serving(rep, n_req):
+def measure_serving(rep, n_req, frames_per_iteration=8):
     """The live serving loop (se_server_start) fed from this thread with Poisson arrivals at
     each of SERVE_RATES, in both modes: continuous batching, and one request at a time with
     one launch per frame (the reference's dispatch).  Each rate replays the same sessions
@@ -568,7 +597,7 @@ def measure_serving(rep, n_req):
             for (s, n, mods, t) in reqs]
 
     def one(rate, plain, budget):
-        srv = Server(rs, budget)
+        srv = Server(rs, budget, frames_per_iteration)
         for (w, h), g in zip(sessions, grids):
             srv.open_session(w, h, g, 1)
         srv.start(plain=plain)
@@ -606,7 +635,7 @@ def measure_serving(rep, n_req):
     return {"workload": f"serve: {n_req} requests per rate, Poisson arrivals at {SERVE_RATES[0]}-{SERVE_RATES[-1]} "
                         f"req/s submitted to the live loop, {len(sessions)} sessions (sides log-uniform in "
                         f"[128, 2048]), N ~ U[1, 600] frames, 0-8 circle edits, twelve_materials rule set, "
-                        f"{SERVE_BUDGET >> 30} GB budget",
+                        f"{SERVE_BUDGET >> 30} GB budget, up to {frames_per_iteration} frames per batched iteration",
             "unit": UNIT, "sweep": sweep, "p99_bound_ms": SERVE_P99_BOUND_MS,
             "sustained_under_bound": {"batched": b, "plain": p,
                                       "speedup": (b / p) if (b and p) else None},
@@ -614,7 +643,7 @@ def measure_serving(rep, n_req):
 
 
 def run_serve(args, rep):
-    m = measure_serving(rep, args.serve_requests)
+    m = measure_serving(rep, args.serve_requests, args.serve_k)
     best = max(m["sweep"], key=lambda r: r["batched"]["throughput"])
     return {
         "metric": METRIC, "value": best["batched"]["throughput"], "unit": UNIT, "n_gpus": rep.world_size,

@@ -108,13 +108,16 @@ World::~World() {
   if (d_color) cudaFree(d_color);
   for (auto* m : mips) cudaFree(m);
   if (d_coords) cudaFree(d_coords);
-  if (copy_stream) cudaStreamSynchronize(copy_stream);
+  for (auto& cs : copy_streams)
+    if (cs) cudaStreamSynchronize(cs);
   for (int i = 0; i < 2; ++i) {
     if (stage[i]) cudaFree(stage[i]);
     if (stage_ready[i]) cudaEventDestroy(stage_ready[i]);
-    if (stage_done[i]) cudaEventDestroy(stage_done[i]);
+    for (auto& e : stage_done[i])
+      if (e) cudaEventDestroy(e);
   }
-  if (copy_stream) cudaStreamDestroy(copy_stream);
+  for (auto& cs : copy_streams)
+    if (cs) cudaStreamDestroy(cs);
   if (d_composite) cudaFree(d_composite);
   if (d_bg) cudaFree(d_bg);
   if (d_scratch) cudaFree(d_scratch);
@@ -547,31 +550,41 @@ Status World::composite(const float* bg, int bw, int bh) {
 }
 
 Status World::read_grid_overlapped(uint32_t* host) {
-  const size_t bytes = (size_t)W * H * sizeof(uint32_t);
-  if (!copy_stream) {
-    SE_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+  const size_t cells = (size_t)W * H, bytes = cells * sizeof(uint32_t);
+  if (!copy_streams[0]) {
+    for (auto& cs : copy_streams) SE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     for (int i = 0; i < 2; ++i) {
       cudaError_t e = cudaMalloc(&stage[i], bytes);
       if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
       SE_CUDA(cudaEventCreateWithFlags(&stage_ready[i], cudaEventDisableTiming));
-      SE_CUDA(cudaEventCreateWithFlags(&stage_done[i], cudaEventDisableTiming));
-      SE_CUDA(cudaEventRecord(stage_done[i], copy_stream));
+      for (int c = 0; c < kCopyStreams; ++c) {
+        SE_CUDA(cudaEventCreateWithFlags(&stage_done[i][c], cudaEventDisableTiming));
+        SE_CUDA(cudaEventRecord(stage_done[i][c], copy_streams[c]));
+      }
     }
   }
   const int i = stage_i;
   stage_i ^= 1;
-  SE_CUDA(cudaStreamWaitEvent(stream, stage_done[i], 0));  // its previous host copy has finished
+  for (int c = 0; c < kCopyStreams; ++c)  // the previous host copy out of this stage has finished
+    SE_CUDA(cudaStreamWaitEvent(stream, stage_done[i][c], 0));
   SE_CUDA(cudaMemcpyAsync(stage[i], buf[cur], bytes, cudaMemcpyDeviceToDevice, stream));
   SE_CUDA(cudaEventRecord(stage_ready[i], stream));
-  SE_CUDA(cudaStreamWaitEvent(copy_stream, stage_ready[i], 0));
-  SE_CUDA(cudaMemcpyAsync(host, stage[i], bytes, cudaMemcpyDeviceToHost, copy_stream));
-  SE_CUDA(cudaEventRecord(stage_done[i], copy_stream));
+  const size_t part = (cells + kCopyStreams - 1) / kCopyStreams;
+  for (int c = 0; c < kCopyStreams; ++c) {
+    const size_t a = std::min(cells, (size_t)c * part), b = std::min(cells, a + part);
+    SE_CUDA(cudaStreamWaitEvent(copy_streams[c], stage_ready[i], 0));
+    if (b > a)
+      SE_CUDA(cudaMemcpyAsync(host + a, stage[i] + a, (b - a) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                              copy_streams[c]));
+    SE_CUDA(cudaEventRecord(stage_done[i][c], copy_streams[c]));
+  }
   return Status::Ok();
 }
 
 Status World::synchronize_all() {
   SE_CUDA(cudaStreamSynchronize(stream));
-  if (copy_stream) SE_CUDA(cudaStreamSynchronize(copy_stream));
+  for (auto& cs : copy_streams)
+    if (cs) SE_CUDA(cudaStreamSynchronize(cs));
   return Status::Ok();
 }
 

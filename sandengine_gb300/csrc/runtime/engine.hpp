@@ -136,9 +136,13 @@ struct World {
   // Grid read-back overlapped with the next frames: the grid is snapshotted on the world's
   // stream (device copy into one of two staging buffers) and copied to the host on a copy
   // stream, so the world's next launches do not wait for the host copy.
+  // The host copy is split over kCopyStreams streams (and so over the device's copy
+  // engines), each carrying one contiguous part of the grid.
+  static constexpr int kCopyStreams = 4;
   uint32_t* stage[2] = {nullptr, nullptr};
-  cudaStream_t copy_stream = nullptr;
-  cudaEvent_t stage_ready[2] = {nullptr, nullptr}, stage_done[2] = {nullptr, nullptr};
+  cudaStream_t copy_streams[kCopyStreams] = {};
+  cudaEvent_t stage_ready[2] = {nullptr, nullptr};
+  cudaEvent_t stage_done[2][kCopyStreams] = {};
   int stage_i = 0;
   Status read_grid_overlapped(uint32_t* host);
   Status synchronize_all();  // the world's stream and the copy stream
