@@ -286,6 +286,112 @@ __device__ __forceinline__ void se_list_push(bool dyn, uint32_t entry, uint16_t*
   if (dyn && se_check(at < cap, 4u)) list[DOWN ? cap - 1 - at : at] = (uint16_t)entry;
 }
 
+// The blocks of rows ly0 + 2 j, j in [0, nby), past the last whole chunk of each row,
+// updated right away.
+template <int SW, int SH, int OX, int NT, bool EDGE>
+__device__ __forceinline__ void se_rem_blocks(uint8_t* sm, int ly0, int nby, int gx0, int gy0, int f, int W, int H,
+                                              const uint16_t* __restrict__ lut) {
+  constexpr int NBX = (SW - OX) / 2, NCX = NBX / 4, REM = NBX - 4 * NCX;
+  if (REM) {
+    for (int t = threadIdx.x; t < nby * REM; t += NT) {
+      const int j = t / REM, r = t - j * REM;
+      const int lx = OX + 2 * (4 * NCX + r), ly = ly0 + 2 * j;
+      if (!se_check((ly + 1) * SW + lx + 1 < SW * SH, 2u)) continue;
+      uint8_t* p = sm + ly * SW + lx;
+      uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+      if ((a | b | c | d) == 0u) continue;
+      const int gx = gx0 + lx, gy = gy0 + ly;
+      se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
+      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, EDGE);
+    }
+  }
+}
+
+// A chunk (rows a0 a1 / b0 b1) that is 16 cells of one material whose block is static.
+__device__ __forceinline__ bool se_uniform_static(uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1,
+                                                  uint32_t umask) {
+  const uint32_t m = a0 & 0xffu;
+  const bool uniform = ((a0 ^ a1) | (a0 ^ b0) | (a0 ^ b1)) == 0u && a0 == m * 0x01010101u;
+  return uniform && ((__funnelshift_rc(umask, 0u, m) & 1u) != 0u);  // umask < 2^16: ids >= 16 read 0
+}
+
+// 16 consecutive cells at p (two chunks' rows).  OX = 0: p is 8-byte aligned (16-byte when
+// SW is a multiple of 16); OX = 1: one byte past that.
+template <int SW, int OX>
+__device__ __forceinline__ void se_ld16(const uint8_t* p, uint32_t& w0, uint32_t& w1, uint32_t& w2, uint32_t& w3) {
+  if (OX == 0 && SW % 16 == 0) {
+    const uint4 v = *reinterpret_cast<const uint4*>(p);
+    w0 = v.x;
+    w1 = v.y;
+    w2 = v.z;
+    w3 = v.w;
+  } else if (OX == 0) {
+    se_ld8<0>(p, w0, w1);
+    se_ld8<0>(p + 8, w2, w3);
+  } else {
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(p - 1);
+    const uint32_t u0 = q[0], u1 = q[1], u2 = q[2], u3 = q[3], u4 = q[4];
+    w0 = __funnelshift_r(u0, u1, 8);
+    w1 = __funnelshift_r(u1, u2, 8);
+    w2 = __funnelshift_r(u2, u3, 8);
+    w3 = __funnelshift_r(u3, u4, 8);
+  }
+}
+
+// Appends `off` for lanes with d0 and `off + 8` for lanes with d1; one atomicAdd per warp.
+__device__ __forceinline__ void se_list_push2(bool d0, bool d1, uint32_t off, uint16_t* __restrict__ list,
+                                              int* __restrict__ cnt, int cap) {
+  const uint32_t m0 = __ballot_sync(0xffffffffu, d0), m1 = __ballot_sync(0xffffffffu, d1);
+  if ((m0 | m1) == 0u) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(cnt, __popc(m0) + __popc(m1));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  int at = base + __popc(m0 & lt) + __popc(m1 & lt);
+  if (d0) {
+    if (se_check(at < cap, 4u)) list[at] = (uint16_t)off;
+    ++at;
+  }
+  if (d1 && se_check(at < cap, 4u)) list[at] = (uint16_t)(off + 8u);
+}
+
+// The collect phase of a tile wholly inside the world, two horizontally adjacent chunks per
+// lane (one pair of loads per row, one list reservation per warp for both): block rows
+// ly0 + 2 j, j in [jlo, jlo + nby).
+template <int SW, int SH, int OX, int NT>
+__device__ __forceinline__ void se_chunk_collect_pairs(uint8_t* sm, int ly0, int jlo, int nby, int gx0, int gy0,
+                                                       int f, int W, int H, const uint16_t* __restrict__ lut,
+                                                       uint32_t umask, uint16_t* __restrict__ list,
+                                                       int* __restrict__ cnt) {
+  static_assert(NT % 32 == 0 || NT == 1, "whole warps");
+  static_assert(SW % 8 == 0 && SW * SH <= 65536, "8-byte rows, 16-bit offsets");
+  constexpr int NBX = (SW - OX) / 2, NCX = NBX / 4, NPX = (NCX + 1) / 2;
+  constexpr int CAP = (SW / 8) * (SH / 2);
+  ly0 += 2 * jlo;
+  const int np = NPX * nby;
+  for (int base = threadIdx.x & ~31; base < np; base += NT) {  // warp-uniform trip count
+    const int pi = base + (threadIdx.x & 31);
+    bool d0 = false, d1 = false;
+    int off = 0;
+    if (pi < np) {
+      const int j = pi / NPX, qp = pi - j * NPX;
+      off = (ly0 + 2 * j) * SW + OX + 16 * qp;
+      // a pair at an odd offset reads up to 19 bytes from off: at most 3 past the row (the
+      // next row, or the 16-byte slack after the array)
+      if (!se_check(off >= 0 && off + SW + 19 <= ((SW * SH + 15) & ~15) + 16, 8u)) off = 0;
+      uint32_t a0, a1, a2, a3, b0, b1, b2, b3;
+      se_ld16<SW, OX>(sm + off, a0, a1, a2, a3);
+      se_ld16<SW, OX>(sm + off + SW, b0, b1, b2, b3);
+      d0 = !se_uniform_static(a0, a1, b0, b1, umask);
+      // an odd chunk count leaves the last pair with one chunk
+      d1 = (NCX % 2 == 0 || 2 * qp + 1 < NCX) && !se_uniform_static(a2, a3, b2, b3, umask);
+    }
+    se_list_push2(d0, d1, (uint32_t)off, list, cnt, CAP);
+  }
+  se_rem_blocks<SW, SH, OX, NT, false>(sm, ly0, nby, gx0, gy0, f, W, H, lut);
+}
+
 // Block rows ly0 + 2 j, j in [jlo, jlo + nby), are collected (the rows a step still needs).
 // In an edge tile (part of the array outside the world) chunks wholly outside the world are
 // left alone, and chunks partly outside go to the far end of the list (counted in bcnt),
@@ -328,19 +434,7 @@ __device__ __forceinline__ void se_chunk_collect(uint8_t* sm, int ly0, int jlo, 
     se_list_push(dyn, (uint32_t)off, list, cnt, CAP);
     if (EDGE) se_list_push<true>(border, (uint32_t)off, list, bcnt, CAP);
   }
-  if (REM) {  // blocks past the last whole chunk of each row
-    for (int t = threadIdx.x; t < nby * REM; t += NT) {
-      const int j = t / REM, r = t - j * REM;
-      const int lx = OX + 2 * (4 * NCX + r), ly = ly0 + 2 * j;
-      if (!se_check((ly + 1) * SW + lx + 1 < SW * SH, 2u)) continue;
-      uint8_t* p = sm + ly * SW + lx;
-      uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
-      if ((a | b | c | d) == 0u) continue;
-      const int gx = gx0 + lx, gy = gy0 + ly;
-      se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
-      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, EDGE);
-    }
-  }
+  se_rem_blocks<SW, SH, OX, NT, EDGE>(sm, ly0, nby, gx0, gy0, f, W, H, lut);
 }
 
 #ifdef SE_LUT
@@ -711,9 +805,9 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
         se_chunk_collect<SW, SH, 1, NT, true>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c, bc);
     } else {
       if (se_off_x(f) == 0)
-        se_chunk_collect<SW, SH, 0, NT, false>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c, bc);
+        se_chunk_collect_pairs<SW, SH, 0, NT>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
       else
-        se_chunk_collect<SW, SH, 1, NT, false>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c, bc);
+        se_chunk_collect_pairs<SW, SH, 1, NT>(sm, ly0, jlo, nby, gx0, gy0, f, W, H, lut, umask, list, c);
     }
     __syncthreads();
     const int n = *c, nb = *bc;

@@ -48,6 +48,10 @@ inline float __uint_as_float(unsigned u) {
   __builtin_memcpy(&f, &u, 4);
   return f;
 }
+inline unsigned __funnelshift_rc(unsigned lo, unsigned hi, unsigned s) {  // shift clamped to 32
+  const unsigned long long v = ((unsigned long long)hi << 32) | lo;
+  return (unsigned)(v >> (s > 32u ? 32u : s));
+}
 inline unsigned __funnelshift_r(unsigned lo, unsigned hi, unsigned s) {
   const unsigned long long v = ((unsigned long long)hi << 32) | lo;
   return (unsigned)(v >> (s & 31));
