@@ -709,6 +709,11 @@ class _SingleRank:
 
 
 def run_reference(args, rep):
+    """The reference's own compute shader compiled for the CPU (the whole shader per
+    invocation, as the reference dispatches it), all host threads, on the workload's own
+    steps: each step is one edit period (60 frames, the step's edit round on the first) of
+    a band of the same world (rows 0..R-1 as a world of their own); only the dispatches are
+    timed.  Without that build, the oracle port."""
     if rep.rank != 0:
         return None
     spec = workload(args.workload)
@@ -725,28 +730,37 @@ def run_reference(args, rep):
         ref = None
         kind = "port"
     port = None if ref else Port(text)
-    rows = 64 if W >= 4096 else W
-    band = np.ascontiguousarray(full[:rows])
+    rows = 16 if W >= 4096 else W  # a few seconds per 60-frame step on 16 cores
+    band = np.ascontiguousarray(full[:rows]).copy()
+    frame = 1
 
-    def one(f):
+    def one(r):
+        nonlocal band, frame
+        mods = [(x, y, sh, rad, m) for (x, y, sh, rad, m) in wl.world_edits(W, r, spec["edit_mats"])
+                if y - rad < rows] if W >= 4096 else None
         if ref:
-            return ref.time_rows(band, f, 0, rows, cores)
-        g = band.copy()
-        t0 = time.perf_counter()
-        port.run(g, f - 1, 1, None, cores)
-        return time.perf_counter() - t0
+            band, secs = ref.run_timed(band, frame, FRAMES_PER_STEP, mods, cores)
+        else:
+            t0 = time.perf_counter()
+            port.run(band, frame, FRAMES_PER_STEP, mods, cores)
+            secs = time.perf_counter() - t0
+        frame += FRAMES_PER_STEP
+        return secs
 
     for i in range(args.warmup):
-        one(2 + i)
-    times = [one(2 + args.warmup + i) for i in range(args.steps)]
-    value = band.size * args.steps / sum(times)
-    sample = f"{spec['name']} rows 0-{rows - 1} ({W} x {rows} band), one frame per step, {cores} threads ({model})"
+        one(i)
+    times = [one(args.warmup + i) for i in range(args.steps)]
+    value = band.size * FRAMES_PER_STEP * args.steps / sum(times)
+    sample = (f"{spec['name']} rows 0-{rows - 1} ({W} x {rows} band of the seeded world as a world of its own), "
+              f"{FRAMES_PER_STEP} frames per step with the step's edits, {cores} threads ({model}); the whole "
+              f"compute shader per invocation (grid update, colour, light)")
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": rep.world_size,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 texels (ids)",
             "data": "synthetic (seeded splitmix64)",
-            "config": {"workload": f"{spec['name']}: {spec['ruleset']} rule set, {spec['fill']}; "
-                                   f"reference compute shader on the CPU, bounded band sample",
+            "config": {"workload": f"{spec['name']}: {spec['ruleset']} rule set, {spec['fill']}, "
+                                   f"{FRAMES_PER_STEP} frames per step, the step's circle edits on the first; "
+                                   f"reference compute shader on the CPU, {W} x {rows} band",
                        "parallelism": "host threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -267,6 +267,28 @@ class Ref:
                                    nthreads, y0, y1)
         return time.perf_counter() - t
 
+    def run_timed(self, grid: np.ndarray, frame0: int, nframes: int, mods=None, nthreads: int = 1):
+        """``nframes`` dispatches with counters frame0 + 1 .. (mods on the first), the data and
+        light textures ping-ponged as the reference's Simulation::run does; returns the new
+        grid and the seconds spent in the dispatches alone."""
+        import time
+        H, W = grid.shape
+        g = grid.astype(np.int64)
+        tex = [np.zeros((H, W, 4), dtype=np.float32) for _ in range(2)]
+        tex[0][..., 0] = np.where(g < (1 << 24), g, (1 << 24) - 1).astype(np.float32)
+        light = [np.zeros((H, W, 4), dtype=np.float32) for _ in range(2)]
+        color = np.zeros((H, W, 4), dtype=np.float32)
+        m = mods_array(mods or [])
+        secs = 0.0
+        for i in range(nframes):
+            a, b = i & 1, (i + 1) & 1
+            t = time.perf_counter()
+            self.lib.ref_dispatch(tex[a].ctypes.data, tex[b].ctypes.data, color.ctypes.data, light[a].ctypes.data,
+                                  light[b].ctypes.data, W, H, frame0 + 1 + i,
+                                  m.ctypes.data if (i == 0 and len(m)) else None, len(m) if i == 0 else 0, nthreads)
+            secs += time.perf_counter() - t
+        return tex[nframes & 1][..., 0].astype(np.int64).astype(np.uint32), secs
+
     def step(self, grid: np.ndarray, frame: int, mods=None, nthreads: int = 1,
              light: Optional[np.ndarray] = None, color: Optional[np.ndarray] = None) -> np.ndarray:
         """One dispatch with counter value ``frame``; returns the new grid (ids as uint32).
