@@ -752,11 +752,10 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int i = i0 + u * NT;
-        if (i < NL) {
-          const int r = i / WPR, c = i - r * WPR;
-          *reinterpret_cast<uint32_t*>(sm + r * SW + 4 * c) =
-              se_norm(v[u].x) | (se_norm(v[u].y) << 8) | (se_norm(v[u].z) << 16) | (se_norm(v[u].w) << 24);
-        }
+        if (i < NL)  // word r * WPR + c of the array is word i (rows are WPR = SW / 4 words)
+          reinterpret_cast<uint32_t*>(sm)[i] =
+              __byte_perm(__byte_perm(se_norm(v[u].x), se_norm(v[u].y), 0x0040),
+                          __byte_perm(se_norm(v[u].z), se_norm(v[u].w), 0x0040), 0x5410);
       }
     }
   } else {
