@@ -67,12 +67,19 @@ SE_EXPORT void ref_dispatch_rows(const float* in_data, float* out_data, float* o
     sim_modifications[i] = s;
   }
   if (nthreads <= 0) nthreads = 1;
+  // work items of 256 invocations along a row, so that bands of a few rows still keep every
+  // thread busy
+  constexpr int kSpan = 256;
+  const long long spans = (W + kSpan - 1) / kSpan, items = (long long)(y1 - y0) * spans;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
-  for (int y = y0; y < y1; ++y)
-    for (int x = 0; x < W; ++x) {
+  for (long long t = 0; t < items; ++t) {
+    const int y = y0 + (int)(t / spans), x0 = (int)(t % spans) * kSpan;
+    const int x1 = x0 + kSpan < W ? x0 + kSpan : W;
+    for (int x = x0; x < x1; ++x) {
       gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
       glsl_main();
     }
+  }
 }
 
 }  // extern "C"
