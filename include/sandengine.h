@@ -200,6 +200,11 @@ int se_world_get_grid_async(se_world* w, uint32_t* cells, size_t count);
  * `cells` holds this grid once se_world_synchronize returns.  At most two such reads are
  * in flight; a third waits for the first.  (No counterpart in the reference.) */
 int se_world_read_grid_overlapped(se_world* w, uint32_t* cells, size_t count);
+/* The same read-back with each cell's material id packed into one byte on the device (a
+ * quarter of the bytes over the host link; rule sets of at most 256 materials).  Ids that
+ * name no material are reported as NULL (1), the value the next frame reads them as; after
+ * any frame every cell already holds a material id, so the bytes then equal the grid. */
+int se_world_read_grid_u8_overlapped(se_world* w, uint8_t* cells, size_t count);
 /* Device pointer of the current grid (valid until the next step, which ping-pongs). */
 int se_world_device_grid(se_world* w, uint32_t** device_cells);
 /* Params.frame (simulation.rs:78): the counter before the next step (>= 0). */

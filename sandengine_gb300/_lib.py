@@ -59,6 +59,7 @@ _SIGS = {
     "se_ruleset_material_id": ([_P, ctypes.c_char_p, ctypes.POINTER(_I)], _I),
     "se_world_set_light": ([_P, _I], _I),
     "se_world_read_grid_overlapped": ([_P, _P, ctypes.c_size_t], _I),
+    "se_world_read_grid_u8_overlapped": ([_P, _P, ctypes.c_size_t], _I),
     "se_world_read_pass_timing": ([_P, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                                    ctypes.POINTER(ctypes.c_longlong)], _I),
     "se_world_get_light": ([_P, _P, ctypes.c_size_t], _I),

@@ -422,6 +422,14 @@ SE_API int se_world_get_grid_async(se_world* w, uint32_t* cells, size_t count) {
   return guard([&] { return grid_copy(w, cells, count, false, false); });
 }
 
+SE_API int se_world_read_grid_u8_overlapped(se_world* w, uint8_t* cells, size_t count) {
+  return guard([&] {
+    if (!w || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");
+    if (count != (size_t)w->w->W * w->w->H) return fail(SE_ERR_INVALID_ARGUMENT, "count must be width * height");
+    return ret(w->w->read_grid_u8_overlapped(cells));
+  });
+}
+
 SE_API int se_world_read_grid_overlapped(se_world* w, uint32_t* cells, size_t count) {
   return guard([&] {
     if (!w || !cells) return fail(SE_ERR_INVALID_ARGUMENT, "null argument");

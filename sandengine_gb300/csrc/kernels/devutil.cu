@@ -55,9 +55,37 @@ __global__ void __launch_bounds__(256) se_histogram_kernel(const uint32_t* __res
     if (local[i]) atomicAdd(&counts[i], (unsigned long long)local[i]);
 }
 
+// out[i] = g[i] < nmat ? g[i] : 1 (the material id as the next frame reads it, unknown ids
+// NULL) as one byte; four cells per thread and step (16-byte load, 4-byte store), then the
+// tail.  nmat <= 256.
+__global__ void __launch_bounds__(256) se_pack_ids_kernel(const uint32_t* __restrict__ g, uint8_t* __restrict__ out,
+                                                          unsigned long long n, uint32_t nmat) {
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long n4 = n / 4;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(g) + i);
+    const uint32_t a = v.x < nmat ? v.x : 1u, b = v.y < nmat ? v.y : 1u, c = v.z < nmat ? v.z : 1u,
+                   d = v.w < nmat ? v.w : 1u;
+    reinterpret_cast<uint32_t*>(out)[i] = __byte_perm(__byte_perm(a, b, 0x0040), __byte_perm(c, d, 0x0040), 0x5410);
+  }
+  for (unsigned long long i = 4 * n4 + (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t v = g[i];
+    out[i] = (uint8_t)(v < nmat ? v : 1u);
+  }
+}
+
 }  // namespace
 
 namespace se::rt {
+
+cudaError_t pack_ids_u8(const uint32_t* g, uint8_t* out, unsigned long long n, uint32_t nmat, cudaStream_t s) {
+  if (nmat < 1 || nmat > 256) return cudaErrorInvalidValue;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  se_pack_ids_kernel<<<sms * 8, 256, 0, s>>>(g, out, n, nmat);
+  return cudaGetLastError();
+}
 
 cudaError_t grid_digest(const uint32_t* g, unsigned long long n, unsigned long long* d_out, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(unsigned long long), s);

@@ -115,6 +115,10 @@ World::~World() {
     if (stage_ready[i]) cudaEventDestroy(stage_ready[i]);
     for (auto& e : stage_done[i])
       if (e) cudaEventDestroy(e);
+    if (stage8[i]) cudaFree(stage8[i]);
+    if (stage8_ready[i]) cudaEventDestroy(stage8_ready[i]);
+    for (auto& e : stage8_done[i])
+      if (e) cudaEventDestroy(e);
   }
   for (auto& cs : copy_streams)
     if (cs) cudaStreamDestroy(cs);
@@ -549,10 +553,50 @@ Status World::composite(const float* bg, int bw, int bh) {
   return Status::Ok();
 }
 
+Status World::ensure_copy_streams() {
+  if (!copy_streams[0])
+    for (auto& cs : copy_streams) SE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  return Status::Ok();
+}
+
+Status World::read_grid_u8_overlapped(uint8_t* host) {
+  const size_t cells = (size_t)W * H;
+  const int nmat = rs->num_materials();
+  if (nmat > 256) return {SE_ERR_INVALID_ARGUMENT, "ids fit a byte only for rule sets of at most 256 materials"};
+  Status st = ensure_copy_streams();
+  if (!st.ok()) return st;
+  if (!stage8[0]) {
+    for (int i = 0; i < 2; ++i) {
+      cudaError_t e = cudaMalloc(&stage8[i], cells);
+      if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+      SE_CUDA(cudaEventCreateWithFlags(&stage8_ready[i], cudaEventDisableTiming));
+      for (int c = 0; c < kCopyStreams; ++c) {
+        SE_CUDA(cudaEventCreateWithFlags(&stage8_done[i][c], cudaEventDisableTiming));
+        SE_CUDA(cudaEventRecord(stage8_done[i][c], copy_streams[c]));
+      }
+    }
+  }
+  const int i = stage8_i;
+  stage8_i ^= 1;
+  for (int c = 0; c < kCopyStreams; ++c)  // the previous host copy out of this stage has finished
+    SE_CUDA(cudaStreamWaitEvent(stream, stage8_done[i][c], 0));
+  SE_CUDA(pack_ids_u8(buf[cur], stage8[i], cells, (uint32_t)nmat, stream));
+  SE_CUDA(cudaEventRecord(stage8_ready[i], stream));
+  const size_t part = (cells + kCopyStreams - 1) / kCopyStreams;
+  for (int c = 0; c < kCopyStreams; ++c) {
+    const size_t a = std::min(cells, (size_t)c * part), b = std::min(cells, a + part);
+    SE_CUDA(cudaStreamWaitEvent(copy_streams[c], stage8_ready[i], 0));
+    if (b > a) SE_CUDA(cudaMemcpyAsync(host + a, stage8[i] + a, b - a, cudaMemcpyDeviceToHost, copy_streams[c]));
+    SE_CUDA(cudaEventRecord(stage8_done[i][c], copy_streams[c]));
+  }
+  return Status::Ok();
+}
+
 Status World::read_grid_overlapped(uint32_t* host) {
   const size_t cells = (size_t)W * H, bytes = cells * sizeof(uint32_t);
-  if (!copy_streams[0]) {
-    for (auto& cs : copy_streams) SE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  Status cs_st = ensure_copy_streams();
+  if (!cs_st.ok()) return cs_st;
+  if (!stage[0]) {
     for (int i = 0; i < 2; ++i) {
       cudaError_t e = cudaMalloc(&stage[i], bytes);
       if (e != cudaSuccess) return {SE_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};

@@ -145,6 +145,14 @@ struct World {
   cudaEvent_t stage_done[2][kCopyStreams] = {};
   int stage_i = 0;
   Status read_grid_overlapped(uint32_t* host);
+  // The same with the ids packed into bytes on the device first (a quarter of the bytes
+  // over the host link); their own staging buffers and events.
+  uint8_t* stage8[2] = {nullptr, nullptr};
+  cudaEvent_t stage8_ready[2] = {nullptr, nullptr};
+  cudaEvent_t stage8_done[2][kCopyStreams] = {};
+  int stage8_i = 0;
+  Status read_grid_u8_overlapped(uint8_t* host);
+  Status ensure_copy_streams();
   Status synchronize_all();  // the world's stream and the copy stream
 };
 
@@ -171,6 +179,8 @@ Status launch_edit_on(const Ruleset& rs, uint32_t* grid, int W, int row0, int ro
 cudaError_t grid_digest(const uint32_t* g, unsigned long long n, unsigned long long* d_out, cudaStream_t s);
 cudaError_t grid_histogram(const uint32_t* g, unsigned long long n, int nbins, unsigned long long* d_counts,
                            cudaStream_t s);
+// Each cell's material id as one byte (unknown ids NULL), nmat <= 256, on stream s.
+cudaError_t pack_ids_u8(const uint32_t* g, uint8_t* out, unsigned long long n, uint32_t nmat, cudaStream_t s);
 int noalloc_max_bins();
 cudaError_t histogram_noalloc(const uint32_t* g, unsigned long long n, int nbins, unsigned long long* host_counts,
                               cudaStream_t s);

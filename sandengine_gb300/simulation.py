@@ -130,6 +130,13 @@ class Simulation:
         assert out.shape == (h, w) and out.dtype == np.uint32 and out.flags.c_contiguous
         check(lib().se_world_read_grid_overlapped(self._h, out.ctypes.data, out.size))
 
+    def read_grid_u8_overlapped(self, out: np.ndarray) -> None:
+        """read_grid_overlapped with the ids packed into bytes ((H, W) uint8); ids that name
+        no material read as NULL (1)."""
+        w, h = self.size
+        assert out.shape == (h, w) and out.dtype == np.uint8 and out.flags.c_contiguous
+        check(lib().se_world_read_grid_u8_overlapped(self._h, out.ctypes.data, out.size))
+
     def device_grid_ptr(self) -> int:
         p = ctypes.c_void_p()
         check(lib().se_world_device_grid(self._h, ctypes.byref(p)))

@@ -200,3 +200,36 @@ def test_overlapped_read_back_returns_each_steps_grid(se, rulesets, ports):
     sim.synchronize()
     for o, w in zip(outs, wants):
         assert np.array_equal(o, w)
+
+
+@pytest.mark.parametrize("shape", [(300, 220), (301, 7)])
+def test_packed_read_back_returns_each_steps_grid(se, rulesets, ports, shape):
+    """se_world_read_grid_u8_overlapped: the ids as bytes, three read-backs in flight over
+    consecutive steps (the third waits for the first's staging buffer), each equal to the
+    oracle's grid of its step; a cell count not a multiple of 4 takes the tail path.  Before
+    any frame, ids that name no material read as NULL (1)."""
+    from sandengine_gb300 import workloads as wl
+    P = ports["twelve_materials"]
+    rs = se.parse_string(rulesets["twelve_materials"])
+    W, H = shape
+    g = wl.patch_fill(W, H, 8, *wl.twelve_fill_spec(), patch=16)
+    g[::5, ::3] = 300  # unknown ids
+    sim = se.Simulation(rs, (W, H))
+    sim.grid = g
+    sim.params.frame = 2
+    first = np.empty((H, W), dtype=np.uint8)
+    sim.read_grid_u8_overlapped(first)
+    sim.synchronize()
+    assert np.array_equal(first, np.where(g < rs.num_materials, g, 1).astype(np.uint8))
+    outs, wants, f = [], [], 2
+    for r in range(3):
+        sim.run_frames(7)
+        P.run(g, f, 7)
+        f += 7
+        o = np.empty((H, W), dtype=np.uint8)
+        sim.read_grid_u8_overlapped(o)
+        outs.append(o)
+        wants.append(g.copy())
+    sim.synchronize()
+    for o, w in zip(outs, wants):
+        assert int(w.max()) < 256 and np.array_equal(o, w.astype(np.uint8))
