@@ -82,13 +82,6 @@ extern "C" __global__ void __launch_bounds__(256) se_build_lut(uint16_t* __restr
     lut[i] = (uint16_t)(a | (b << 4) | (c << 8) | (d << 12));
   }
 }
-// Tables up to this size are copied into shared memory by each CTA.
-#define SE_LUT_SMEM_MAX_ENTRIES 16384u
-#if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
-#define SE_LUT_SMEM_BYTES ((SE_LUT_ENTRIES * 2u + 15u) & ~15u)
-#else
-#define SE_LUT_SMEM_BYTES 0u
-#endif
 // The bitset of static keys follows the table at this byte offset.  Bit `key` is set when
 // the table maps the block with that key to itself for every hash value.
 #define SE_LUT_STATIC_OFF ((SE_LUT_ENTRIES * 2u + 15u) & ~15u)
@@ -139,11 +132,7 @@ __device__ __forceinline__ void se_block_update(uint32_t& a, uint32_t& b, uint32
   const uint32_t h0 = se_mix(x * 213u), h1 = se_mix(x * 2131u), h2 = se_mix(x * 21313u), h3 = se_mix(x * 213132u);
   uint32_t idx = se_gen::lut_index(a, b, c, d, h0, h1, h2, h3);
   if (!se_check(idx < SE_LUT_ENTRIES, 1u)) idx = 0;
-#if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
-  const uint32_t o = lut[idx];  // shared-memory copy
-#else
   const uint32_t o = __ldg(lut + idx);
-#endif
   a = o & 15u;
   b = (o >> 4) & 15u;
   c = (o >> 8) & 15u;
@@ -171,9 +160,6 @@ __device__ __forceinline__ void se_block_store(uint8_t* p, int SW, uint32_t a, u
   }
 }
 
-#ifndef SE_LUT
-#define SE_LUT_SMEM_BYTES 0u
-#endif
 // Every tile runs each step in two phases over chunks of four horizontally adjacent
 // blocks (8 cells x 2 rows):
 //  1. se_chunk_collect reads every chunk with two 8-byte loads.  A chunk whose 16 cells are
@@ -190,7 +176,7 @@ __device__ __forceinline__ void se_block_store(uint8_t* p, int SW, uint32_t a, u
 // Chunks are skipped whole, so the lanes that evaluate blocks do so together rather than
 // waiting on one another; blocks of one step are disjoint, so the list order is free.
 
-// Shared-memory layout after the cell array and the table copy: 16 bytes of slack (chunk
+// Shared-memory layout after the cell array: 16 bytes of slack (chunk
 // loads at odd offsets read up to 3 bytes past a row), the list counters of alternate steps
 // (chunks to evaluate, then chunks with cells outside the world, which fill the list from
 // its far end), one flag byte per material id < 16, then the list.
@@ -263,11 +249,7 @@ __device__ __forceinline__ uint32_t se_lut_word_index(uint32_t abcd, uint32_t x)
 }
 __device__ __forceinline__ uint32_t se_lut_fetch(const uint16_t* __restrict__ lut, uint32_t idx) {
   if (!se_check(idx < SE_LUT_ENTRIES, 1u)) idx = 0;
-#if SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
-  return lut[idx];
-#else
   return __ldg(lut + idx);
-#endif
 }
 #endif
 
@@ -553,20 +535,6 @@ __device__ __forceinline__ void se_step_rt(uint8_t* sm, int SW, int SH, int ox, 
   }
 }
 
-// Copies a small block transition table into shared memory at byte offset `off`;
-// returns the table to use.
-__device__ __forceinline__ const uint16_t* se_lut_to_smem(const uint16_t* __restrict__ lut, uint8_t* smem, int off,
-                                                         int nt) {
-#if defined(SE_LUT) && SE_LUT_ENTRIES <= SE_LUT_SMEM_MAX_ENTRIES
-  uint16_t* slut = reinterpret_cast<uint16_t*>(smem + off);
-  for (uint32_t i = threadIdx.x; i < SE_LUT_ENTRIES / 2u; i += nt)
-    reinterpret_cast<uint32_t*>(slut)[i] = __ldg(reinterpret_cast<const uint32_t*>(lut) + i);
-  return slut;
-#else
-  return lut;
-#endif
-}
-
 // Loads rows [gy0, gy0 + SH) x columns [gx0, gx0 + SW) of a W x H grid into the u8 array
 // (row stride SW, a multiple of 4; gx0 a multiple of 4): ids normalised, outside = WALL.
 __device__ __forceinline__ void se_load_region(uint8_t* sm, int SW, int SH, const uint32_t* __restrict__ src, int W,
@@ -720,13 +688,12 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   extern __shared__ __align__(16) uint8_t se_smem[];
   uint8_t* sm = se_smem;
   se_gen::init_tables(threadIdx.x, NT);
-  constexpr int HDR = ((SW * SH + 15) & ~15) + (int)SE_LUT_SMEM_BYTES;
+  constexpr int HDR = (SW * SH + 15) & ~15;
   int* cnt = reinterpret_cast<int*>(se_smem + HDR + SE_HDR_CNT);
   uint8_t* flags = se_smem + HDR + SE_HDR_FLAGS;
   uint16_t* list = reinterpret_cast<uint16_t*>(se_smem + HDR + SE_HDR_LIST);
   for (int i = threadIdx.x; i < 4; i += NT) cnt[i] = 0;  // [s & 1]: to evaluate, [2 + (s & 1)]: border
   se_uniform_flags(lut, flags, NT);
-  lut = se_lut_to_smem(lut, se_smem, (SW * SH + 15) & ~15, NT);
   const int gx0 = X0 - HX, gy0 = Y0 - HY;
   const bool vec = (W & 3) == 0;
 
@@ -919,7 +886,6 @@ extern "C" __global__ void __launch_bounds__(1024) se_resident(const SeWorldDesc
   const int SW = ((w.W + 3) & ~3) + 8, SH = w.H + 2;
   const int gx0 = -4, gy0 = -1;
   se_gen::init_tables(threadIdx.x, blockDim.x);
-  lut = se_lut_to_smem(lut, se_smem, (SW * SH + 15) & ~15, blockDim.x);
   const uint32_t* src = w.cur ? w.buf1 : w.buf0;
   uint32_t* dst = (w.cur ^ out_flip) ? w.buf1 : w.buf0;
   se_load_region(se_smem, SW, SH, src, w.W, w.H, gx0, gy0, blockDim.x);

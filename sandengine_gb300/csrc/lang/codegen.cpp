@@ -1086,9 +1086,15 @@ bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err) {
     bool lut = g.nmat <= 16;
     for (const char* t : {"pos_x", "pos_y", "frame", "sim_w", "sim_h", "se_randf"}) lut = lut && !has_tok(t);
     g.bounds[0].insert(0x7fffffc0ull);
-    const int bits = g.nmat <= 2 ? 1 : g.nmat <= 4 ? 2 : g.nmat <= 8 ? 3 : 4;
-    uint64_t entries = 1ull << (4 * bits);
-    for (int l = 0; l < 4; ++l) entries *= g.bounds[l].size() + 1;
+    uint64_t classes = 1;
+    for (int l = 0; l < 4; ++l) classes *= g.bounds[l].size() + 1;
+    // Ids take 4 bits of the key whenever that table fits: the tile kernel then builds two
+    // blocks' keys from a row pair with one permute, and no table is copied into shared
+    // memory (a small table's copy costs CTAs per SM and its lookups conflict in the banks).
+    // Otherwise the fewest bits that hold every id.
+    const int min_bits = g.nmat <= 2 ? 1 : g.nmat <= 4 ? 2 : g.nmat <= 8 ? 3 : 4;
+    const int bits = (classes << 16) <= (1ull << 24) ? 4 : min_bits;
+    const uint64_t entries = (1ull << (4 * bits)) * classes;
     if (entries > (1ull << 24)) lut = false;
     const uint64_t keys = 1ull << (4 * bits);
     if (lut) {

@@ -169,13 +169,9 @@ Module::~Module() {
   if (lib) cudaLibraryUnload(lib);
 }
 
-size_t lut_smem_bytes(const LutShape& lut) {
-  if (lut.entries && lut.entries <= kLutSmemMaxEntries) return ((size_t)lut.entries * 2 + 15) & ~(size_t)15;
-  return 0;
-}
-
 size_t tile_smem_bytes(const TileVariant& t, const LutShape& lut) {
-  size_t b = ((t.smem_bytes() + 15) & ~(size_t)15) + lut_smem_bytes(lut);
+  (void)lut;
+  size_t b = (t.smem_bytes() + 15) & ~(size_t)15;
   // 48-byte header (slack, list counters, uniform-material flags), then the per-step list
   // of chunks (4 blocks) to evaluate, one u16 offset each
   b += 48 + ((2 * (size_t)(t.sw() / 8) * (size_t)(t.sh() / 2) + 15) & ~(size_t)15);

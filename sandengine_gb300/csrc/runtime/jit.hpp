@@ -25,20 +25,14 @@ struct TileVariant {
 };
 const std::vector<TileVariant>& tile_variants();
 
-// Block transition tables up to this many entries are copied into shared memory by each
-// CTA (SE_LUT_SMEM_MAX_ENTRIES in kernels/margolus.cuh); larger ones are read from global
-// memory through the read-only cache.
-constexpr unsigned long long kLutSmemMaxEntries = 16384;
 // Size of a rule set's block transition table: its u16 entries and the 32-bit words of the
 // bitset of static keys that follows it (both 0 without a table).
 struct LutShape {
   unsigned long long entries = 0, static_words = 0;
 };
-// Shared memory the table copy of a CTA takes (the table when it fits, rounded up to 16
-// bytes).  The static-key bitset stays in global memory.
-size_t lut_smem_bytes(const LutShape& lut);
-// Dynamic shared memory of a tile launch: the u8 tile, then the table copy, then the
-// per-step list of chunks to evaluate.
+// Dynamic shared memory of a tile launch: the u8 tile, then the per-step list of chunks to
+// evaluate.  The block transition table and its static-key bitset stay in global memory
+// (read through the read-only cache).
 size_t tile_smem_bytes(const TileVariant& t, const LutShape& lut);
 
 // Full device source: prelude + generated rules + kernel template + instantiations.

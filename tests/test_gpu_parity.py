@@ -134,6 +134,36 @@ def test_direct_path_matches_port(se, rulesets):
         assert np.array_equal(sim.grid, a), f"k={k}"
 
 
+def test_narrow_table_keys_match_port(se):
+    """A rule set with 544 hash classes keys its table with 3 bits per id (the generic key
+    build); one-frame and fused launches must be exact too, and the device-built table must
+    equal the one the same device code builds on the CPU."""
+    import ctypes
+    from oracle.build import Port
+    from sandengine_gb300 import workloads as wl
+    from tests.device_emu.emu import Emu
+    with open(os.path.join(GOLDEN, "many_hash_classes.yaml")) as f:
+        text = f.read()
+    rs = se.parse_string(text)
+    assert "#define SE_LUT_BITS 3" in rs.cuda_source
+    table, bits = rs.table()
+    E = Emu(rs, lut=True)
+    E.lib.emu_lut.restype = ctypes.POINTER(ctypes.c_uint16)
+    assert np.array_equal(table, np.ctypeslib.as_array(E.lib.emu_lut(), shape=(table.size,)))
+    port = Port(text)
+    w, h = 203, 131
+    g = wl.iid_fill(w, h, 6, *wl.FOUR_FILL)
+    for k in (1, 8):
+        sim = se.Simulation(rs, (w, h))
+        sim.set_steps_per_launch(k)
+        a = g.copy()
+        sim.grid = a
+        sim.params.frame = 3
+        sim.run_frames(45)
+        port.run(a, 3, 45)
+        assert np.array_equal(sim.grid, a), f"k={k}"
+
+
 def test_frame_one_clears(se, rulesets):
     g = np.full((40, 40), 3, dtype=np.uint32)
     sim = _sim(se, rulesets["four_materials"], 40, 40)

@@ -110,12 +110,47 @@ def test_edits_inside_the_fused_launch_match_port(emus, ports, name, variant):
         assert np.array_equal(got, want), f"frame {f}: {int(np.count_nonzero(got != want))} cells differ"
 
 
-@pytest.mark.parametrize("name", ["four_materials", "twelve_materials"])
+def _narrow_keys_text():
+    """A rule set with 544 hash classes: its table keys take 3 bits per id (4-bit keys would
+    make the table larger than 2^24 entries)."""
+    import os
+    from tests.conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "many_hash_classes.yaml")) as f:
+        return f.read()
+
+
+def _text(rulesets, name):
+    return _narrow_keys_text() if name == "many_hash_classes" else rulesets[name]
+
+
+@pytest.mark.parametrize("lut", [True, False], ids=["table", "direct"])
+def test_narrow_table_keys_match_port(se, lut):
+    """Every tile variant with 3-bit table keys (the generic key build of the collect and
+    eval phases) against the port, on ragged worlds."""
+    from oracle.build import Port
+    text = _narrow_keys_text()
+    rs = se.parse_string(text)
+    assert "#define SE_LUT_BITS 3" in rs.kernel_source
+    E, P = Emu(rs, lut=lut), Port(text)
+    for w, h in [(130, 67), (517, 389)]:
+        g0 = wl.iid_fill(w, h, 4, *wl.FOUR_FILL)
+        for v in VARIANTS:
+            a, f0 = g0.copy(), 5
+            for rep in range(2):
+                k = max(1, v[2] - rep)
+                b = E.tiles(a, f0, k, v)
+                P.run(a, f0 - 1, k)
+                f0 += k
+                assert np.array_equal(a, b), f"{w}x{h} variant {v} k={k}: {np.count_nonzero(a != b)} cells differ"
+                a = b
+
+
+@pytest.mark.parametrize("name", ["four_materials", "twelve_materials", "many_hash_classes"])
 def test_static_key_bitset(se, rulesets, name):
     """Bit `key` of se_build_static's bitset is set exactly when every table entry of that
     key maps the block to itself; the all-EMPTY key is always static."""
     import ctypes
-    rs = se.parse_string(rulesets[name])
+    rs = se.parse_string(_text(rulesets, name))
     E = Emu(rs, lut=True)
     assert E.has_lut
     src = rs.kernel_source
@@ -206,13 +241,13 @@ def test_rules_that_set_wall_cells_keep_the_world_border(se, rulesets, ports):
         assert np.array_equal(got, want), f"serving {W}x{H}"
 
 
-@pytest.mark.parametrize("name", ["four_materials", "twelve_materials"])
+@pytest.mark.parametrize("name", ["four_materials", "twelve_materials", "many_hash_classes"])
 def test_lut_index_classes_at_every_boundary(se, rulesets, name):
     """lut_index_key's class per hash lane equals #{thresholds <= h} at every threshold and
     its neighbours, every multiple of 2^24 and its predecessor, 0 and 2^32 - 1."""
     import ctypes
     import re
-    rs = se.parse_string(rulesets[name])
+    rs = se.parse_string(_text(rulesets, name))
     src = rs.kernel_source
     dec = src[src.index("lut_decode("):]
     dec = dec[:dec.index("\n}\n")]
