@@ -211,18 +211,32 @@ __device__ __forceinline__ uint32_t se_flags_mask(const uint8_t* flags) {
   return (m0 & 15u) | ((m1 & 15u) << 4) | ((m2 & 15u) << 8) | ((m3 & 15u) << 12);
 }
 
-// 8 consecutive cells at p.  OX = 0: p is 8-byte aligned; OX = 1: one byte past that.
+// True when p is a multiple of `align` bytes (a CHECKED-build check of vector accesses).
+__device__ __forceinline__ bool se_aligned(const void* p, unsigned align) {
+  return (reinterpret_cast<unsigned long long>(p) & (align - 1u)) == 0u;
+}
+
+// 8 consecutive cells at p.  OX = 0: p is 8-byte aligned; OX = 1: one byte past that (an
+// 8-byte load from p - 1 and a 4-byte load after it).
 template <int OX>
 __device__ __forceinline__ void se_ld8(const uint8_t* p, uint32_t& lo, uint32_t& hi) {
   if (OX == 0) {
+    if (!se_check(se_aligned(p, 8), 2u)) {
+      lo = hi = 0x02020202u;
+      return;
+    }
     const uint2 v = *reinterpret_cast<const uint2*>(p);
     lo = v.x;
     hi = v.y;
   } else {
-    const uint32_t* q = reinterpret_cast<const uint32_t*>(p - 1);
-    const uint32_t w0 = q[0], w1 = q[1], w2 = q[2];
-    lo = __funnelshift_r(w0, w1, 8);
-    hi = __funnelshift_r(w1, w2, 8);
+    if (!se_check(se_aligned(p - 1, 8), 2u)) {
+      lo = hi = 0x02020202u;
+      return;
+    }
+    const uint2 v = *reinterpret_cast<const uint2*>(p - 1);
+    const uint32_t w2 = *reinterpret_cast<const uint32_t*>(p + 7);
+    lo = __funnelshift_r(v.x, v.y, 8);
+    hi = __funnelshift_r(v.y, w2, 8);
   }
 }
 template <int OX>
@@ -301,6 +315,10 @@ __device__ __forceinline__ bool se_uniform_static(uint32_t a0, uint32_t a1, uint
 // SW is a multiple of 16); OX = 1: one byte past that.
 template <int SW, int OX>
 __device__ __forceinline__ void se_ld16(const uint8_t* p, uint32_t& w0, uint32_t& w1, uint32_t& w2, uint32_t& w3) {
+  if (SW % 16 == 0 && !se_check(se_aligned(p - OX, 16), 2u)) {
+    w0 = w1 = w2 = w3 = 0x02020202u;
+    return;
+  }
   if (OX == 0 && SW % 16 == 0) {
     const uint4 v = *reinterpret_cast<const uint4*>(p);
     w0 = v.x;
@@ -310,6 +328,13 @@ __device__ __forceinline__ void se_ld16(const uint8_t* p, uint32_t& w0, uint32_t
   } else if (OX == 0) {
     se_ld8<0>(p, w0, w1);
     se_ld8<0>(p + 8, w2, w3);
+  } else if (SW % 16 == 0) {  // p - 1 is 16-byte aligned: one 16-byte load and the word after it
+    const uint4 v = *reinterpret_cast<const uint4*>(p - 1);
+    const uint32_t u4 = *reinterpret_cast<const uint32_t*>(p + 15);
+    w0 = __funnelshift_r(v.x, v.y, 8);
+    w1 = __funnelshift_r(v.y, v.z, 8);
+    w2 = __funnelshift_r(v.z, v.w, 8);
+    w3 = __funnelshift_r(v.w, u4, 8);
   } else {
     const uint32_t* q = reinterpret_cast<const uint32_t*>(p - 1);
     const uint32_t u0 = q[0], u1 = q[1], u2 = q[2], u3 = q[3], u4 = q[4];
