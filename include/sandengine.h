@@ -240,8 +240,9 @@ int se_world_histogram(se_world* w, uint64_t* counts, int nbins);
  * the device) the next call looks it up again.  Every call shares the array: it clears
  * the counters on `cuda_stream` (NULL = the legacy default stream), counts, copies nbins
  * counters to host_counts and synchronizes the stream before returning, so calls from one
- * thread never overlap; calls from different threads or streams that overlap on the GPU
- * race on the counters.  (No counterpart in the reference.) */
+ * thread never overlap, and no call may be made on a stream that is being captured into a
+ * graph; calls from different threads or streams that overlap on the GPU race on the
+ * counters.  (No counterpart in the reference.) */
 #define SE_NOALLOC_MAX_BINS 257
 int se_grid_histogram_noalloc(const uint32_t* device_cells, uint64_t count, int nbins, uint64_t* host_counts,
                               void* cuda_stream);
