@@ -532,34 +532,6 @@ __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __
   }
 }
 
-// The same over a shared array whose size is only known at run time (whole worlds); the
-// block index is split with a float reciprocal and a +-1 correction.
-__device__ __forceinline__ void se_step_rt(uint8_t* sm, int SW, int SH, int ox, int ly0, int gx0, int gy0, int f,
-                                           int W, int H, const uint16_t* __restrict__ lut) {
-  const int nbx = (SW - ox) / 2;
-  const int nb = nbx * ((SH - ly0) / 2);
-  const float inv = 1.0f / (float)nbx;
-  for (int bi = threadIdx.x; bi < nb; bi += blockDim.x) {
-    int j = __float2int_rz((float)bi * inv);
-    int i = bi - j * nbx;
-    if (i >= nbx) {
-      ++j;
-      i -= nbx;
-    } else if (i < 0) {
-      --j;
-      i += nbx;
-    }
-    const int lx = ox + 2 * i, ly = ly0 + 2 * j;
-    if (!se_check(ly >= 0 && lx >= 0 && (ly + 1) * SW + lx + 1 < SW * SH, 2u)) continue;
-    uint8_t* p = sm + ly * SW + lx;
-    uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
-    if ((a | b | c | d) == 0u) continue;
-    const int gx = gx0 + lx, gy = gy0 + ly;
-    se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
-    se_block_store(p, SW, a, b, c, d, gx, gy, W, H, true);
-  }
-}
-
 // Loads rows [gy0, gy0 + SH) x columns [gx0, gx0 + SW) of a W x H grid into the u8 array
 // (row stride SW, a multiple of 4; gx0 a multiple of 4): ids normalised, outside = WALL.
 __device__ __forceinline__ void se_load_region(uint8_t* sm, int SW, int SH, const uint32_t* __restrict__ src, int W,
@@ -899,25 +871,158 @@ __device__ __forceinline__ void se_stile_impl(const SeWorldDesc* __restrict__ de
   se_tile_run<TW, TH, KMAX, NT>(src, dst, w.W, w.H, w.frame + 1, w.pad0, lut, tx * TW, ty * TH, 0, w.H);
 }
 
+// A chunk of a whole world in shared memory at array offset `off` (row ly, column lx; the
+// array's cell (0, 0) is world cell (gx0, gy0)), all of its cells inside the world.
+template <int OX>
+__device__ __forceinline__ void se_rt_chunk(uint8_t* sm, int SW, int off, int ly, int lx, int gx0, int gy0, int f,
+                                            int W, int H, const uint16_t* __restrict__ lut) {
+#ifdef SE_LUT
+  (void)W, (void)H;
+  const uint32_t x = (uint32_t)(gx0 + lx) * 461u + (uint32_t)(gy0 + ly) * 2131u + (uint32_t)f * 4541161u;
+  se_chunk_eval<OX>(sm + off, SW, x, lut);
+#else
+  (void)lut;
+  for (int kb = 0; kb < 4; ++kb) {  // the generated rules, block by block
+    uint8_t* p = sm + off + 2 * kb;
+    uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+    if ((a | b | c | d) == 0u) continue;
+    se_block(a, b, c, d, gx0 + lx + 2 * kb, gy0 + ly, f, W, H);
+    p[0] = (uint8_t)a;
+    p[1] = (uint8_t)b;
+    p[SW] = (uint8_t)c;
+    p[SW + 1] = (uint8_t)d;
+  }
+#endif
+}
+
+// j = i / n and i - j n for 0 <= i < 2^22 (a float reciprocal and a +-1 correction).
+__device__ __forceinline__ void se_divmod_rt(int i, int n, float inv, int& j, int& r) {
+  j = __float2int_rz((float)i * inv);
+  r = i - j * n;
+  if (r >= n) {
+    ++j;
+    r -= n;
+  } else if (r < 0) {
+    --j;
+    r += n;
+  }
+}
+
+// One frame of a whole world held in shared memory (se_resident's array: row stride SW, a
+// multiple of 8; rows ly0 + 2 j are the block rows), as the tile kernel's edge tiles run
+// a step: the collect phase lists the chunks of world cells that are not uniform static
+// (entries are array offset / 8, which fits 16 bits for any array that fits in shared
+// memory) and puts the chunks with cells outside the world at the far end of the list;
+// after a barrier the listed chunks are evaluated word-wide and the border chunks block by
+// block, their cells outside the world kept WALL; the blocks of a row past its last whole
+// chunk are updated in the collect phase.  cnt[0] / cnt[1] count the two ends of the list;
+// the caller zeroes them before the step, and `next` (the other step's pair) is zeroed here
+// once the counts are read.
+template <int OX>
+__device__ __forceinline__ void se_rt_step(uint8_t* sm, int SW, int SH, int ly0, int gx0, int gy0, int f, int W,
+                                           int H, const uint16_t* __restrict__ lut, uint32_t umask,
+                                           uint16_t* __restrict__ list, int cap, int* cnt, int* next) {
+  const int nt = blockDim.x;
+  const int nbx = (SW - OX) / 2, ncx = nbx / 4, rem = nbx - 4 * ncx, nby = (SH - ly0) / 2;
+  const int nc = ncx * nby, sw8 = SW >> 3;
+  const float inv_ncx = 1.0f / (float)ncx, inv_sw8 = 1.0f / (float)sw8;
+  for (int base = threadIdx.x & ~31; base < nc; base += nt) {  // warp-uniform trip count
+    const int ci = base + (threadIdx.x & 31);
+    bool dyn = false, border = false;
+    uint32_t e = 0;
+    if (ci < nc) {
+      int j, q;
+      se_divmod_rt(ci, ncx, inv_ncx, j, q);
+      const int ly = ly0 + 2 * j, lx = OX + 8 * q;
+      const int off = ly * SW + lx;
+      e = (uint32_t)(off >> 3);
+      const int gx = gx0 + lx, gy = gy0 + ly;
+      const bool inside = gx >= 0 && gx + 7 < W && gy >= 0 && gy + 1 < H;
+      border = !inside && gx + 7 >= 0 && gx < W && gy + 1 >= 0 && gy < H;
+      if (inside && se_check(off + SW + 11 <= ((SW * SH + 15) & ~15) + 16, 8u)) {
+        uint32_t a0, a1, b0, b1;
+        se_ld8<OX>(sm + off, a0, a1);
+        se_ld8<OX>(sm + off + SW, b0, b1);
+        dyn = !se_uniform_static(a0, a1, b0, b1, umask);
+      }
+    }
+    se_list_push(dyn, e, list, cnt, cap);
+    se_list_push<true>(border, e, list, cnt + 1, cap);
+  }
+  for (int t = threadIdx.x; t < nby * rem; t += nt) {  // blocks past the last whole chunk of a row
+    const int j = t / rem, r = t - j * rem;
+    const int lx = OX + 2 * (4 * ncx + r), ly = ly0 + 2 * j;
+    if (!se_check((ly + 1) * SW + lx + 1 < SW * SH, 2u)) continue;
+    uint8_t* p = sm + ly * SW + lx;
+    uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+    if ((a | b | c | d) == 0u) continue;
+    const int gx = gx0 + lx, gy = gy0 + ly;
+    se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
+    se_block_store(p, SW, a, b, c, d, gx, gy, W, H, true);
+  }
+  __syncthreads();
+  const int n = cnt[0], nb = cnt[1];
+  if (threadIdx.x == 0) next[0] = next[1] = 0;  // last read in the previous step
+  for (int i = threadIdx.x; i < n; i += nt) {
+    if (!se_check(i < cap, 4u)) break;
+    int ly, q;
+    se_divmod_rt(list[i], sw8, inv_sw8, ly, q);
+    const int lx = OX + 8 * q, off = ly * SW + lx;
+    if (!se_check(off >= 0 && off + SW + 11 <= ((SW * SH + 15) & ~15) + 16, 8u)) continue;
+    se_rt_chunk<OX>(sm, SW, off, ly, lx, gx0, gy0, f, W, H, lut);
+  }
+  for (int i = threadIdx.x; i < nb; i += nt) {  // chunks with cells outside the world
+    if (!se_check(i < cap, 4u)) break;
+    int ly, q;
+    se_divmod_rt(list[cap - 1 - i], sw8, inv_sw8, ly, q);
+    const int lx = OX + 8 * q;
+    if (!se_check(ly >= 0 && (ly + 1) * SW + lx + 7 < SW * SH, 8u)) continue;
+    for (int kb = 0; kb < 4; ++kb) {
+      uint8_t* p = sm + ly * SW + lx + 2 * kb;
+      uint32_t a = p[0], b = p[1], c = p[SW], d = p[SW + 1];
+      if ((a | b | c | d) == 0u) continue;  // all EMPTY stays EMPTY
+      const int gx = gx0 + lx + 2 * kb, gy = gy0 + ly;
+      se_block_update(a, b, c, d, gx, gy, f, W, H, lut);
+      se_block_store(p, SW, a, b, c, d, gx, gy, W, H, true);
+    }
+  }
+}
+
 // Whole-world launch: CTA b holds world ids[b] entirely in shared memory (plus a WALL
-// border: 4 columns each side for aligned loads, 1 row above and below), advances it by
-// `frames` frames and stores it to the buffer cur ^ out_flip.  Nothing outside the world is
-// ever written back, so the border stays WALL for every frame, as getCell returns there.
+// border: 4 columns on the left and at least 4 on the right, the row stride a multiple of
+// 8; 1 row above and below), advances it by `frames` frames and stores it to the buffer
+// cur ^ out_flip.  Nothing outside the world is ever written back, so the border stays
+// WALL for every frame, as getCell returns there.  After the array (rounded up to 16
+// bytes): 16 bytes of slack, the list counters of alternate frames, the uniform-material
+// flags, then the chunk list (SE_HDR_* offsets, as in the tile kernel), one entry per chunk.
 extern "C" __global__ void __launch_bounds__(1024) se_resident(const SeWorldDesc* __restrict__ worlds,
                                                                const int* __restrict__ ids, int frames, int out_flip,
                                                                const uint16_t* __restrict__ lut) {
   extern __shared__ __align__(16) uint8_t se_smem[];
   const SeWorldDesc w = worlds[ids[blockIdx.x]];
-  const int SW = ((w.W + 3) & ~3) + 8, SH = w.H + 2;
+  const int SW = ((w.W + 7) & ~7) + 8, SH = w.H + 2;
   const int gx0 = -4, gy0 = -1;
+  const int HDR = (SW * SH + 15) & ~15, cap = (SW / 8) * (SH / 2);
+  int* cnt = reinterpret_cast<int*>(se_smem + HDR + SE_HDR_CNT);
+  uint8_t* flags = se_smem + HDR + SE_HDR_FLAGS;
+  uint16_t* list = reinterpret_cast<uint16_t*>(se_smem + HDR + SE_HDR_LIST);
   se_gen::init_tables(threadIdx.x, blockDim.x);
+  for (int i = threadIdx.x; i < 4; i += blockDim.x) cnt[i] = 0;
+  se_uniform_flags(lut, flags, blockDim.x);
   const uint32_t* src = w.cur ? w.buf1 : w.buf0;
   uint32_t* dst = (w.cur ^ out_flip) ? w.buf1 : w.buf0;
   se_load_region(se_smem, SW, SH, src, w.W, w.H, gx0, gy0, blockDim.x);
   __syncthreads();
+  const uint32_t umask = se_flags_mask(flags);
   for (int s = 0; s < frames; ++s) {
     const int f = w.frame + 1 + s;
-    se_step_rt(se_smem, SW, SH, se_off_x(f), (se_off_y(f) + gy0) & 1, gx0, gy0, f, w.W, w.H, lut);
+    const int ly0 = (se_off_y(f) + gy0) & 1;
+    int* c = cnt + 2 * (s & 1);
+    int* nx = cnt + 2 * ((s + 1) & 1);
+    if (se_off_x(f) == 0)
+      se_rt_step<0>(se_smem, SW, SH, ly0, gx0, gy0, f, w.W, w.H, lut, umask, list, cap, c, nx);
+    else
+      se_rt_step<1>(se_smem, SW, SH, ly0, gx0, gy0, f, w.W, w.H, lut, umask, list, cap, c, nx);
     __syncthreads();
   }
   se_store_region(se_smem, SW, 4, 1, w.W, w.H, dst, w.W, w.H, 0, 0, blockDim.x);

@@ -19,10 +19,13 @@ Status cuda_fail(const char* what, cudaError_t e) {
     if (_e != cudaSuccess) return cuda_fail(#call, _e); \
   } while (0)
 
+// Shared memory of a whole world in se_resident: the array (row stride a multiple of 8, a
+// WALL border), a 48-byte header and a chunk list of one u16 entry per chunk.
 size_t resident_bytes(int W, int H, const LutShape& lut) {
-  size_t b = (size_t)(((W + 3) & ~3) + 8) * (size_t)(H + 2);
   (void)lut;
-  return (b + 15) & ~(size_t)15;
+  const size_t SW = (size_t)(((W + 7) & ~7) + 8), SH = (size_t)H + 2;
+  const size_t cap = (SW / 8) * (SH / 2);
+  return ((SW * SH + 15) & ~(size_t)15) + 48 + ((2 * cap + 15) & ~(size_t)15);
 }
 }  // namespace
 
