@@ -69,6 +69,11 @@ Status Server::create(std::shared_ptr<Ruleset> r, long long budget_bytes) {
 Status Server::set_frames_per_iteration(int k) {
   std::lock_guard<std::mutex> g(mu);
   if (live) return {SE_ERR_INVALID_ARGUMENT, "the frames per iteration cannot change while the server runs"};
+  // The first compiled variant with the fewest frames >= k: for k = 8 the 128x64 tiles,
+  // which serve sessions of 128-2048 cells a side best (the serving benchmark's highest
+  // throughput, 770 G cell-updates/s, against 690-734 G with 256x128, 128x128 or 256x64
+  // tiles): their smaller halo loss on the large tiles does not make up for the waste on
+  // the small sessions and the coarser work units of an iteration.
   const TileVariant* v = nullptr;
   for (const TileVariant& t : tile_variants())
     if (t.kmax >= k && (!v || t.kmax < v->kmax)) v = &t;
