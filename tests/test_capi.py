@@ -29,6 +29,9 @@ def test_bad_arguments_return_status(se):
     assert L.se_ruleset_parse(None, ctypes.byref(out)) == 1
     assert b"null" in L.se_last_error()
     assert L.se_world_step(None, 1, None, 0) == 1
+    host = ctypes.create_string_buffer(64)
+    assert L.se_world_read_grid_u8_overlapped(None, host, 16) == 1  # null world
+    assert L.se_world_read_grid_overlapped(None, host, 16) == 1
     assert L.se_ruleset_text(None, 0, None, 0, None) == 1
     rs = se.parse_string(open(os.path.join(ROOT, "sandengine_gb300", "rulesets", "four_materials.yaml")).read())
     assert L.se_ruleset_text(rs.handle, 9, None, 0, None) == 1

@@ -263,3 +263,9 @@ def test_packed_read_back_returns_each_steps_grid(se, rulesets, ports, shape):
     sim.synchronize()
     for o, w in zip(outs, wants):
         assert int(w.max()) < 256 and np.array_equal(o, w.astype(np.uint8))
+    # a buffer of the wrong size is refused with a status, before any copy
+    import ctypes
+    from sandengine_gb300._lib import lib
+    small = np.empty(W * H - 1, dtype=np.uint8)
+    assert lib().se_world_read_grid_u8_overlapped(sim.handle, small.ctypes.data, small.size) == 1
+    assert b"width * height" in lib().se_last_error()
