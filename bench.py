@@ -550,31 +550,6 @@ def run_batch(args, rep):
     }
 
 
-def serve_workload(rate, n_requests, seed=5):
-    """Poisson arrivals at `rate` req/s; each request opens a new session (p=0.5) or reuses an
-    earlier one; sides log-uniform in [128, 2048] (multiples of 32); N ~ U[1, 600] frames;
-    0-8 circle edits (radius 8-64, EMPTY or sand) on the first frame."""
-    from sandengine_gb300 import workloads as wl
-    u = wl.uniform53(seed, 9, np.arange(8 * n_requests, dtype=np.uint64)).astype(np.float64) / float(1 << 53)
-    u = u.reshape(n_requests, 8)
-    t = np.cumsum(-np.log1p(-u[:, 0]) / rate) * 1e3  # ms
-    sessions, reqs = [], []
-    for i in range(n_requests):
-        if not sessions or u[i, 1] < 0.5:
-            w = int(np.clip(np.round(np.exp(np.log(128) + u[i, 2] * np.log(16)) / 32) * 32, 128, 2048))
-            h = int(np.clip(np.round(np.exp(np.log(128) + u[i, 3] * np.log(16)) / 32) * 32, 128, 2048))
-            sessions.append((w, h))
-            s = len(sessions) - 1
-        else:
-            s = int(u[i, 1] * 2 * len(sessions)) % len(sessions)
-        n = 1 + int(u[i, 4] * 600)
-        ne = int(u[i, 5] * 9)
-        w, h = sessions[s]
-        mods = wl.circle_edits(w, h, seed, i, ne, [0, 3]) if ne else []
-        reqs.append((s, n, mods, float(t[i])))
-    return sessions, reqs
-
-
 SERVE_RATES = (100, 300, 1000, 3000, 10000, 20000)
 SERVE_P99_BOUND_MS = 100.0
 SERVE_BUDGET = 150 << 30
@@ -585,7 +560,7 @@ def measure_serving(rep, n_req, frames_per_iteration=8):
     """The live serving loop (se_server_start) fed from this thread with Poisson arrivals at
     each of SERVE_RATES, in both modes: continuous batching, and one request at a time with
     one launch per frame (the reference's dispatch).  Each rate replays the same sessions
-    and requests (serve_workload), only the arrival times scale.  Per mode: the highest
+    and requests (workloads.serve_requests), only the arrival times scale.  Per mode: the highest
     throughput whose p99 latency stays within SERVE_P99_BOUND_MS.  Then one rate under a
     256 MB budget, so that sessions are evicted to host memory and restored."""
     import sandengine_gb300 as se
@@ -593,8 +568,8 @@ def measure_serving(rep, n_req, frames_per_iteration=8):
     from sandengine_gb300.serving import Server
     rs = se.parse_string(wl.ruleset_text("twelve_materials"))
     spec = wl.twelve_fill_spec()
-    sessions, reqs = serve_workload(1.0, n_req)  # arrival times at 1 req/s; scaled per rate
-    grids = [wl.patch_fill(w, h, 3000 + i, *spec, patch=64) for i, (w, h) in enumerate(sessions)]
+    sessions, reqs = wl.serve_requests(1.0, n_req)  # arrival times at 1 req/s; scaled per rate
+    grids = [wl.serve_session_grid(w, h, i) for i, (w, h) in enumerate(sessions)]
     subs = [(s, n, [se.SimModification((m[0], m[1]), m[2], m[3], m[4]) for m in mods], t)
             for (s, n, mods, t) in reqs]
 

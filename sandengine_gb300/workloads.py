@@ -124,3 +124,36 @@ def world_edits(size: int, round_idx: int, materials: Sequence[int] = (0, 3)):
     """The edit round ``round_idx`` of the size^2 patch world: 32 circles (radius 8-64,
     uniform positions, EMPTY or sand), applied on the first frame of every 60."""
     return circle_edits(size, size, 2, round_idx, WORLD_EDITS_PER_ROUND, materials)
+
+
+# ---- the serving workload ----------------------------------------------------------------
+
+def serve_requests(rate: float, n_requests: int, seed: int = 5):
+    """The serving workload: Poisson arrivals at ``rate`` req/s; each request opens a new
+    session (p = 0.5) or reuses an earlier one; sides log-uniform in [128, 2048] (multiples of
+    32); N ~ U[1, 600] frames; 0-8 circle edits (radius 8-64, EMPTY or sand) on the first
+    frame.  Returns the session sizes and the requests (session, frames, edits, arrival ms)."""
+    u = uniform53(seed, 9, np.arange(8 * n_requests, dtype=np.uint64)).astype(np.float64) / float(1 << 53)
+    u = u.reshape(n_requests, 8)
+    t = np.cumsum(-np.log1p(-u[:, 0]) / rate) * 1e3  # ms
+    sessions, reqs = [], []
+    for i in range(n_requests):
+        if not sessions or u[i, 1] < 0.5:
+            w = int(np.clip(np.round(np.exp(np.log(128) + u[i, 2] * np.log(16)) / 32) * 32, 128, 2048))
+            h = int(np.clip(np.round(np.exp(np.log(128) + u[i, 3] * np.log(16)) / 32) * 32, 128, 2048))
+            sessions.append((w, h))
+            s = len(sessions) - 1
+        else:
+            s = int(u[i, 1] * 2 * len(sessions)) % len(sessions)
+        n = 1 + int(u[i, 4] * 600)
+        ne = int(u[i, 5] * 9)
+        w, h = sessions[s]
+        mods = circle_edits(w, h, seed, i, ne, [0, 3]) if ne else []
+        reqs.append((s, n, mods, float(t[i])))
+    return sessions, reqs
+
+
+def serve_session_grid(width: int, height: int, index: int) -> np.ndarray:
+    """The initial grid of serving session ``index`` (frame counter 1): twelve materials in
+    64x64 patches, seed 3000 + index."""
+    return patch_fill(width, height, 3000 + index, *twelve_fill_spec(), patch=64)
