@@ -594,6 +594,7 @@ def measure_serving(rep, n_req, frames_per_iteration=8):
         return {"throughput": rep.sum(st["cell_updates"] / (st["wall_ms"] / 1e3)),
                 "p50_ms": rep.max(st["p50_ms"]), "p99_ms": rep.max(st["p99_ms"]),
                 "offered_req_s": len(subs) / span, "wall_ms": st["wall_ms"], "iterations": st["iterations"],
+                "gpu_busy": st["kernel_ms"] / st["wall_ms"] if st["wall_ms"] > 0 else None,
                 "evictions": st["evictions"], "restores": st["restores"], "restore_ms": st["restore_ms"]}
 
     sweep = []

@@ -312,6 +312,10 @@ typedef struct se_server_stats {
   long long evictions, restores;
   long long peak_resident_bytes;
   double restore_ms;           /* mean host time to bring an evicted session back into HBM */
+  double kernel_ms;            /* GPU time of the last run's iterations, each from its first launch
+                                  to its end (iterations run in order on one stream, so the gaps
+                                  between them are left out: kernel_ms / wall_ms is the share of the
+                                  run the GPU spent serving) */
 } se_server_stats;
 
 /* A server whose sessions' grids (two u32 buffers each) share one HBM arena of

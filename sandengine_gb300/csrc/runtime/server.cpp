@@ -255,22 +255,29 @@ Status Server::begin_run() {
   iterations = 0;
   cell_updates = 0;
   wall_ms = 0;
+  kernel_ms = 0;
   SE_CUDA(cudaEventRecord(t0, stream));
   SE_CUDA(cudaEventSynchronize(t0));
   host_t0 = Clock::now();
   return Status::Ok();
 }
 
-Status Server::record_iteration(std::vector<int> completes) {
-  cudaEvent_t ev;
+cudaEvent_t Server::take_event() {
+  cudaEvent_t ev = nullptr;
   if (!event_pool.empty()) {
     ev = event_pool.back();
     event_pool.pop_back();
-  } else {
-    SE_CUDA(cudaEventCreate(&ev));
+  } else if (cudaEventCreate(&ev) != cudaSuccess) {
+    ev = nullptr;
   }
+  return ev;
+}
+
+Status Server::record_iteration(std::vector<int> completes, cudaEvent_t start) {
+  cudaEvent_t ev = take_event();
+  if (!ev) return cuda_fail("cudaEventCreate", cudaGetLastError());
   SE_CUDA(cudaEventRecord(ev, stream));
-  inflight.push_back({ev, std::move(completes)});
+  inflight.push_back({ev, std::move(completes), start});
   return Status::Ok();
 }
 
@@ -293,6 +300,12 @@ Status Server::retire(std::unique_lock<std::mutex>& lk, bool all) {
       requests[(size_t)r].done_ms = ms;
     }
     wall_ms = std::max(wall_ms, (double)ms);
+    if (cudaEvent_t st = inflight.front().start) {
+      float k = 0;
+      SE_CUDA(cudaEventElapsedTime(&k, st, ev));
+      kernel_ms += k;
+      event_pool.push_back(st);
+    }
     event_pool.push_back(ev);
     inflight.pop_front();
     any = true;
@@ -539,6 +552,9 @@ Status Server::serve_batched(std::unique_lock<std::mutex>& lk) {
     SE_CUDA(cudaMemcpyAsync(stg.d_desc, stg.desc, active.size() * sizeof(WorldDesc), cudaMemcpyHostToDevice, stream));
     SE_CUDA(cudaMemcpyAsync(stg.d_prefix, stg.prefix, (active.size() + 1) * sizeof(int), cudaMemcpyHostToDevice,
                             stream));
+    cudaEvent_t started = take_event();
+    if (!started) return cuda_fail("cudaEventCreate", cudaGetLastError());
+    SE_CUDA(cudaEventRecord(started, stream));
     {
       const WorldDesc* dd = stg.d_desc;
       const int* pp = stg.d_prefix;
@@ -572,7 +588,7 @@ Status Server::serve_batched(std::unique_lock<std::mutex>& lk) {
     }
     std::vector<int> completes;
     for (int sid : done) finish(sid, completes);
-    st = record_iteration(std::move(completes));
+    st = record_iteration(std::move(completes), started);
     if (!st.ok()) return st;
     active.swap(still);
     st = throttle(lk, 2);
@@ -632,6 +648,9 @@ Status Server::serve_plain(std::unique_lock<std::mutex>& lk) {
     Session& ss = sessions[(size_t)sid];
     Request& r = requests[(size_t)ri];
     r.started = true;
+    cudaEvent_t started = take_event();
+    if (!started) return cuda_fail("cudaEventCreate", cudaGetLastError());
+    SE_CUDA(cudaEventRecord(started, stream));
     for (int i = 0; i < r.remaining; ++i) {
       const int f = ss.frame + 1;
       if (f == 1) {
@@ -651,7 +670,7 @@ Status Server::serve_plain(std::unique_lock<std::mutex>& lk) {
     r.remaining = 0;
     ++iterations;
     ss.last_use = iterations;
-    st = record_iteration({ri});
+    st = record_iteration({ri}, started);
     if (!st.ok()) return st;
     st = throttle(lk, 2);
     if (!st.ok()) return st;
@@ -718,6 +737,7 @@ Status Server::stats(se_server_stats* out) {
   out->restores = restores;
   out->restore_ms = restores ? restore_ms_total / (double)restores : 0.0;
   out->peak_resident_bytes = (long long)peak_used;
+  out->kernel_ms = kernel_ms;
   return Status::Ok();
 }
 

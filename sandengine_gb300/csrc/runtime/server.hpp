@@ -84,6 +84,7 @@ struct Server {
   struct Inflight {
     cudaEvent_t ev;
     std::vector<int> completes;
+    cudaEvent_t start = nullptr;  // recorded before the iteration's first launch, if any
   };
   std::deque<Inflight> inflight;
   std::vector<cudaEvent_t> event_pool;
@@ -91,6 +92,7 @@ struct Server {
   double cell_updates = 0;
   double wall_ms = 0;
   double restore_ms_total = 0;  // host time spent restoring evicted sessions
+  double kernel_ms = 0;         // GPU time of the last run's iterations (first launch to end)
 
   // live loop
   std::mutex mu;
@@ -131,7 +133,9 @@ struct Server {
   Status serve_batched(std::unique_lock<std::mutex>& lk);
   Status serve_plain(std::unique_lock<std::mutex>& lk);
   Status stage_reserve(Stage& st, size_t n);
-  Status record_iteration(std::vector<int> completes);
+  cudaEvent_t take_event();
+  // Records the end of an iteration (whose first launch followed `start`, when not null).
+  Status record_iteration(std::vector<int> completes, cudaEvent_t start = nullptr);
   // Retires finished iterations (all of them when `all`, waiting for the GPU with the lock
   // released), stamping their requests' completion times.
   Status retire(std::unique_lock<std::mutex>& lk, bool all);

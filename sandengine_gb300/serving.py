@@ -32,7 +32,8 @@ class ServerStats(ctypes.Structure):
                 ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("wall_ms", ctypes.c_double),
                 ("cell_updates", ctypes.c_double), ("iterations", ctypes.c_longlong),
                 ("evictions", ctypes.c_longlong), ("restores", ctypes.c_longlong),
-                ("peak_resident_bytes", ctypes.c_longlong), ("restore_ms", ctypes.c_double)]
+                ("peak_resident_bytes", ctypes.c_longlong), ("restore_ms", ctypes.c_double),
+                ("kernel_ms", ctypes.c_double)]
 
 
 class Server:

@@ -61,6 +61,8 @@ def test_mixed_equals_alone_equals_oracle(se, ports, rulesets):
     st = mixed.stats()
     assert st["requests"] == len(reqs) and st["iterations"] > 0
     assert st["p99_ms"] >= st["p50_ms"] >= 0
+    # the iterations' GPU time lies within the run (they run in order on one stream)
+    assert 0 < st["kernel_ms"] <= st["wall_ms"] * 1.001
     assert all(mixed.latency_ms(r) >= 0 for r in ids)
 
 
