@@ -103,7 +103,9 @@ int se_ruleset_num_materials(const se_ruleset* rs, int* n);
 int se_ruleset_material_id(const se_ruleset* rs, const char* name, int* id);
 /* The block transition table this device built for the rule set (no counterpart in the
  * reference, whose shader evaluates the rules per block; this is introspection for
- * tests).  *entries gets the number of u16 entries and *static_words the 32-bit words of
+ * tests).  An entry holds the block's four output ids, 4 bits each, as top-left |
+ * bottom-left << 4 | top-right << 8 | bottom-right << 12.  *entries gets the number of u16
+ * entries and *static_words the 32-bit words of
  * the bitset of static keys (both 0 when the rules need the direct path); when `table` /
  * `bits` are not null, at most cap_entries / cap_words of them are copied from the device.
  * Loads the kernels on the current device first. */

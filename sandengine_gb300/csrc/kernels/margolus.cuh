@@ -69,8 +69,10 @@ __device__ __forceinline__ void se_block(uint32_t& a, uint32_t& b, uint32_t& c, 
 
 #ifdef SE_LUT
 // Fills the block transition table: entry i holds the four output ids (4 bits each) of
-// the block and hash intervals that se_gen::lut_index maps to i.  Keys naming an id >=
-// SE_NMAT never occur (cells are normalised on load) and keep their input.
+// the block and hash intervals that se_gen::lut_index maps to i, as a | c << 4 | b << 8 |
+// d << 12 (top-left, bottom-left, top-right, bottom-right: the bytes of two entries side
+// by side are then the block's columns, see se_chunk_eval).  Keys naming an id >= SE_NMAT
+// never occur (cells are normalised on load) and keep their input.
 extern "C" __global__ void __launch_bounds__(256) se_build_lut(uint16_t* __restrict__ lut) {
   se_gen::init_tables(threadIdx.x, blockDim.x);
   __syncthreads();
@@ -79,7 +81,7 @@ extern "C" __global__ void __launch_bounds__(256) se_build_lut(uint16_t* __restr
     se_gen::lut_decode(i, a, b, c, d, h0, h1, h2, h3);
     if (a < SE_NMAT && b < SE_NMAT && c < SE_NMAT && d < SE_NMAT && (a | b | c | d) != 0u)
       se_rules_hashed(a, b, c, d, h0, h1, h2, h3, 0, 0, 0, 0, 0);  // the rules read no position
-    lut[i] = (uint16_t)(a | (b << 4) | (c << 8) | (d << 12));
+    lut[i] = (uint16_t)(a | (c << 4) | (b << 8) | (d << 12));
   }
 }
 // The bitset of static keys follows the table at this byte offset.  Bit `key` is set when
@@ -98,7 +100,7 @@ extern "C" __global__ void __launch_bounds__(256) se_build_static(uint16_t* __re
     const uint32_t key = w * 32u + j;
     const uint32_t a = key & M, b = (key >> SE_LUT_BITS) & M, c = (key >> (2 * SE_LUT_BITS)) & M,
                    d = (key >> (3 * SE_LUT_BITS)) & M;
-    const uint32_t self = a | (b << 4) | (c << 8) | (d << 12);
+    const uint32_t self = a | (c << 4) | (b << 8) | (d << 12);  // se_build_lut's entry layout
     bool same = true;
     for (uint32_t q = 0; q < C; ++q) same = same && lut[key * C + q] == self;
     if (same) word |= 1u << j;
@@ -134,8 +136,8 @@ __device__ __forceinline__ void se_block_update(uint32_t& a, uint32_t& b, uint32
   if (!se_check(idx < SE_LUT_ENTRIES, 1u)) idx = 0;
   const uint32_t o = __ldg(lut + idx);
   a = o & 15u;
-  b = (o >> 4) & 15u;
-  c = (o >> 8) & 15u;
+  c = (o >> 4) & 15u;  // entry layout a | c << 4 | b << 8 | d << 12 (se_build_lut)
+  b = (o >> 8) & 15u;
   d = o >> 12;
 #else
   se_block(a, b, c, d, gx, gy, f, W, H);
@@ -471,14 +473,12 @@ __device__ __forceinline__ void se_chunk_eval(uint8_t* p, int SW, uint32_t x, co
 #endif
   const uint32_t o0 = se_lut_fetch(lut, i0), o1 = se_lut_fetch(lut, i1), o2 = se_lut_fetch(lut, i2),
                  o3 = se_lut_fetch(lut, i3);
-  // Entries are nibbles a | b << 4 | c << 8 | d << 12.  Two blocks' entries side by side,
-  // split into even and odd nibbles, permute into the top row [a, b, a', b'] and the
-  // bottom row [c, d, c', d'].
+  // Entries are a | c << 4 | b << 8 | d << 12: a block's bytes are its columns [a|c, b|d].
+  // Two blocks' entries side by side are [a|c, b|d, a'|c', b'|d']; their low nibbles are
+  // the top row [a, b, a', b'] and their high nibbles the bottom row [c, d, c', d'].
   const uint32_t P01 = __byte_perm(o0, o1, 0x5410), P23 = __byte_perm(o2, o3, 0x5410);
-  const uint32_t E01 = P01 & 0x0f0f0f0fu, O01 = (P01 >> 4) & 0x0f0f0f0fu;
-  const uint32_t E23 = P23 & 0x0f0f0f0fu, O23 = (P23 >> 4) & 0x0f0f0f0fu;
-  se_st8<OX>(p, __byte_perm(E01, O01, 0x6240), __byte_perm(E23, O23, 0x6240));
-  se_st8<OX>(p + SW, __byte_perm(E01, O01, 0x7351), __byte_perm(E23, O23, 0x7351));
+  se_st8<OX>(p, P01 & 0x0f0f0f0fu, P23 & 0x0f0f0f0fu);
+  se_st8<OX>(p + SW, (P01 >> 4) & 0x0f0f0f0fu, (P23 >> 4) & 0x0f0f0f0fu);
 }
 #endif
 

@@ -168,7 +168,7 @@ def test_static_key_bitset(se, rulesets, name):
     m = (1 << bits) - 1
     k = np.arange(keys, dtype=np.uint32)
     a, b, c, d = k & m, (k >> bits) & m, (k >> (2 * bits)) & m, (k >> (3 * bits)) & m
-    self_ = a | (b << 4) | (c << 8) | (d << 12)
+    self_ = a | (c << 4) | (b << 8) | (d << 12)  # the table's entry layout
     want = np.all(lut == self_[:, None], axis=1)
     got = ((st[k >> 5] >> (k & 31)) & 1).astype(bool)
     assert np.array_equal(got, want)
