@@ -98,9 +98,10 @@ extern "C" __global__ void __launch_bounds__(256) se_build_static(uint16_t* __re
   uint32_t word = 0;
   for (uint32_t j = 0; j < 32u && w * 32u + j < SE_LUT_KEYS; ++j) {
     const uint32_t key = w * 32u + j;
-    const uint32_t a = key & M, b = (key >> SE_LUT_BITS) & M, c = (key >> (2 * SE_LUT_BITS)) & M,
+    // se_gen::lut_key's column order, and se_build_lut's entry layout (the same order)
+    const uint32_t a = key & M, c = (key >> SE_LUT_BITS) & M, b = (key >> (2 * SE_LUT_BITS)) & M,
                    d = (key >> (3 * SE_LUT_BITS)) & M;
-    const uint32_t self = a | (c << 4) | (b << 8) | (d << 12);  // se_build_lut's entry layout
+    const uint32_t self = a | (c << 4) | (b << 8) | (d << 12);
     bool same = true;
     for (uint32_t q = 0; q < C; ++q) same = same && lut[key * C + q] == self;
     if (same) word |= 1u << j;
@@ -458,11 +459,11 @@ __device__ __forceinline__ void se_chunk_eval(uint8_t* p, int SW, uint32_t x, co
   // all-EMPTY blocks (the table maps them to themselves), so the four lookups are in flight
   // together.
 #if SE_LUT_BITS == 4
-  // A row word holds 4 cells (< 16 each); in w | w >> 4, byte 0 is the left block's
-  // left | right << 4 and byte 2 the right block's, so one permute of the two rows' words
-  // gives both blocks' keys (key0 | key1 << 16).
-  const uint32_t k01 = __byte_perm(a0 | (a0 >> 4), b0 | (b0 >> 4), 0x6240);
-  const uint32_t k23 = __byte_perm(a1 | (a1 >> 4), b1 | (b1 >> 4), 0x6240);
+  // A row word holds 4 cells (< 16 each), so top + (bottom << 4) holds in byte j the column
+  // top_j | bottom_j << 4, and its two halves are the two blocks' keys in se_gen::lut_key's
+  // column order (key0 | key1 << 16); the nibbles do not overlap, so the sum is an OR.
+  const uint32_t k01 = b0 * 16u + a0;
+  const uint32_t k23 = b1 * 16u + a1;
   const uint32_t i0 = se_lut_key_index(k01 & 0xffffu, x), i1 = se_lut_key_index(k01 >> 16, x + 922u);
   const uint32_t i2 = se_lut_key_index(k23 & 0xffffu, x + 1844u), i3 = se_lut_key_index(k23 >> 16, x + 2766u);
 #else

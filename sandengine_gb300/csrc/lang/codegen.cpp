@@ -1101,8 +1101,11 @@ bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err) {
       o << "#define SE_LUT 1\n#define SE_LUT_BITS " << bits << "\n#define SE_LUT_ENTRIES " << entries << "u\n"
         << "#define SE_LUT_KEYS " << keys << "u\n#define SE_LUT_STATIC_WORDS " << std::max<uint64_t>(1, keys / 32)
         << "u\n";
+      // The key of the block [a b / c d] (top-left, top-right, bottom-left, bottom-right) in
+      // column order, a | c << bits | b << 2 bits | d << 3 bits: with 4 bits, a row pair's
+      // two keys are its top row word plus its bottom row word << 4 (se_chunk_eval).
       o << "__device__ __forceinline__ uint32_t lut_key(uint32_t a, uint32_t b, uint32_t c, uint32_t d) {\n"
-        << "  return a | (b << " << bits << ") | (c << " << 2 * bits << ") | (d << " << 3 * bits << ");\n}\n";
+        << "  return a | (c << " << bits << ") | (b << " << 2 * bits << ") | (d << " << 3 * bits << ");\n}\n";
       o << "__device__ __forceinline__ uint32_t lut_index_key(uint32_t i, uint32_t h0, uint32_t h1, uint32_t h2, "
            "uint32_t h3) {\n";
       for (int l = 0; l < 4; ++l) {
@@ -1127,7 +1130,7 @@ bool generate_cuda(const ParsingResult& r, CudaRules* out, ParseError* err) {
         o << "}; h" << l << " = reps[i % " << n << "u]; i /= " << n << "u; }\n";
       }
       const uint32_t mask = (1u << bits) - 1;
-      o << "  a = i & " << mask << "u; b = (i >> " << bits << ") & " << mask << "u; c = (i >> " << 2 * bits
+      o << "  a = i & " << mask << "u; c = (i >> " << bits << ") & " << mask << "u; b = (i >> " << 2 * bits
         << ") & " << mask << "u; d = (i >> " << 3 * bits << ") & " << mask << "u;\n}\n";
     }
     o << "}  // namespace se_gen\n";

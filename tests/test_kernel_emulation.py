@@ -167,7 +167,7 @@ def test_static_key_bitset(se, rulesets, name):
     lut = np.ctypeslib.as_array(E.lib.emu_lut(), shape=(entries,)).reshape(keys, C).astype(np.uint32)
     m = (1 << bits) - 1
     k = np.arange(keys, dtype=np.uint32)
-    a, b, c, d = k & m, (k >> bits) & m, (k >> (2 * bits)) & m, (k >> (3 * bits)) & m
+    a, c, b, d = k & m, (k >> bits) & m, (k >> (2 * bits)) & m, (k >> (3 * bits)) & m  # column order
     self_ = a | (c << 4) | (b << 8) | (d << 12)  # the table's entry layout
     want = np.all(lut == self_[:, None], axis=1)
     got = ((st[k >> 5] >> (k & 31)) & 1).astype(bool)
