@@ -309,9 +309,11 @@ __device__ __forceinline__ void se_rem_blocks(uint8_t* sm, int ly0, int nby, int
 // A chunk (rows a0 a1 / b0 b1) that is 16 cells of one material whose block is static.
 __device__ __forceinline__ bool se_uniform_static(uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1,
                                                   uint32_t umask) {
-  const uint32_t m = a0 & 0xffu;
-  const bool uniform = ((a0 ^ a1) | (a0 ^ b0) | (a0 ^ b1)) == 0u && a0 == m * 0x01010101u;
-  return uniform && ((__funnelshift_rc(umask, 0u, m) & 1u) != 0u);  // umask < 2^16: ids >= 16 read 0
+  // all 16 bytes equal: the four words equal, and a0 equal to its byte 0 broadcast
+  const uint32_t diff = (a0 ^ a1) | (a0 ^ b0) | (a0 ^ b1) | (a0 ^ __byte_perm(a0, 0u, 0x0000));
+  // for a uniform chunk a0 & 31 is its material (< 16; the wrapping funnel shift reads
+  // only those bits), and bit m of umask (< 2^16) its static flag
+  return diff == 0u && (__funnelshift_r(umask, 0u, a0) & 1u) != 0u;
 }
 
 // 16 consecutive cells at p (two chunks' rows).  OX = 0: p is 8-byte aligned (16-byte when
@@ -509,15 +511,21 @@ template <int SW, int SH, int OX, int NT>
 __device__ __forceinline__ void se_chunk_process(uint8_t* sm, const uint16_t* __restrict__ list, int n, int gx0,
                                                  int gy0, int f, int W, int H, const uint16_t* __restrict__ lut) {
   const uint32_t xf = (uint32_t)f * 4541161u;
+  // the hash base (gx0 + lx) 461 + (gy0 + ly) 2131 + f 4541161 of the chunk at offset
+  // off = ly SW + lx is xb + 461 off + (2131 - 461 SW) ly (mod 2^32)
+  const uint32_t xb = (uint32_t)gx0 * 461u + (uint32_t)gy0 * 2131u + xf;
+  constexpr uint32_t XROW = 2131u - 461u * (uint32_t)SW;
   for (int i = threadIdx.x; i < n; i += NT) {
     if (!se_check(i < (SW / 8) * (SH / 2), 4u)) break;
     const int off = list[i];
     if (!se_check(off + SW + 11 <= ((SW * SH + 15) & ~15) + 16, 8u)) continue;
     const int ly = off / SW, lx = off - ly * SW;
 #ifdef SE_LUT
-    const uint32_t x = (uint32_t)(gx0 + lx) * 461u + (uint32_t)(gy0 + ly) * 2131u + xf;
+    (void)lx, (void)W, (void)H;
+    const uint32_t x = xb + (uint32_t)off * 461u + (uint32_t)ly * XROW;
     se_chunk_eval<OX>(sm + off, SW, x, lut);
 #else
+    (void)xb;
     (void)xf;
     for (int kb = 0; kb < 4; ++kb) {  // the generated rules, block by block
       uint8_t* p = sm + off + 2 * kb;
