@@ -725,10 +725,17 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int i = i0 + u * NT;
-        if (i < NL)  // word r * WPR + c of the array is word i (rows are WPR = SW / 4 words)
-          reinterpret_cast<uint32_t*>(sm)[i] =
-              __byte_perm(__byte_perm(se_norm(v[u].x), se_norm(v[u].y), 0x0040),
-                          __byte_perm(se_norm(v[u].z), se_norm(v[u].w), 0x0040), 0x5410);
+        if (i < NL) {  // word r * WPR + c of the array is word i (rows are WPR = SW / 4 words)
+          // one unsigned maximum tells whether all four ids name materials (after the first
+          // launch they always do); only otherwise is each id mapped (unknown -> NULL)
+          const uint32_t mx = max(max(v[u].x, v[u].y), max(v[u].z, v[u].w));
+          uint32_t packed = __byte_perm(__byte_perm(v[u].x, v[u].y, 0x0040), __byte_perm(v[u].z, v[u].w, 0x0040),
+                                        0x5410);
+          if (mx >= (uint32_t)SE_NMAT)
+            packed = __byte_perm(__byte_perm(se_norm(v[u].x), se_norm(v[u].y), 0x0040),
+                                 __byte_perm(se_norm(v[u].z), se_norm(v[u].w), 0x0040), 0x5410);
+          reinterpret_cast<uint32_t*>(sm)[i] = packed;
+        }
       }
     }
   } else {
@@ -797,6 +804,18 @@ __device__ __forceinline__ void se_tile_run(const uint32_t* __restrict__ src, ui
   }
 
   constexpr int OWPR = TW / 4;
+  if (vec && X0 + TW <= W && Y0 + TH <= yb && Y0 >= ya) {
+    // the interior lies inside the world and the buffer: no bounds to check
+    uint32_t* out0 = dst + (size_t)(Y0 - ya) * W + X0;
+    for (int i = threadIdx.x; i < OWPR * TH; i += NT) {
+      const int r = i / OWPR, c = i - r * OWPR;
+      const uint32_t packed = *reinterpret_cast<const uint32_t*>(sm + (r + HY) * SW + HX + 4 * c);
+      *reinterpret_cast<uint4*>(out0 + (size_t)r * W + 4 * c) =
+          make_uint4(__byte_perm(packed, 0u, 0x4440), __byte_perm(packed, 0u, 0x4441),
+                     __byte_perm(packed, 0u, 0x4442), __byte_perm(packed, 0u, 0x4443));
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < OWPR * TH; i += NT) {
     const int r = i / OWPR, c = i - r * OWPR;
     const int gy = Y0 + r, gx = X0 + 4 * c;

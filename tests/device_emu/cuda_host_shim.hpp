@@ -72,6 +72,7 @@ inline T __shfl_sync(unsigned, T v, int) { return v; }
 template <class T>
 inline T __shfl_up_sync(unsigned, T v, unsigned) { return v; }  // lane 0: its own value
 inline int __popc(unsigned v) { return __builtin_popcount(v); }
+inline unsigned max(unsigned a, unsigned b) { return a > b ? a : b; }
 inline int __ffs(unsigned v) { return __builtin_ffs((int)v); }
 inline unsigned atomicOr(unsigned* p, unsigned v) {
   const unsigned old = *p;
