@@ -165,8 +165,10 @@ __device__ __forceinline__ void se_block_store(uint8_t* p, int SW, uint32_t a, u
 
 // Every tile runs each step in two phases over chunks of four horizontally adjacent
 // blocks (8 cells x 2 rows):
-//  1. se_chunk_collect reads every chunk with two 8-byte loads.  A chunk whose 16 cells are
-//     one material m whose block of four m cells never changes is left as it is (with a
+//  1. The collect phase reads every chunk: in a tile inside the world two adjacent chunks
+//     per lane with one 16-byte load per row (se_chunk_collect_pairs), else one chunk per
+//     lane with two 8-byte loads (se_chunk_collect).  A chunk whose 16 cells are one
+//     material m whose block of four m cells never changes is left as it is (with a
 //     transition table: EMPTY, and in a typical rule set the solids and liquids at rest;
 //     without one: EMPTY, which the shader itself leaves alone); the others are appended
 //     to a list of array offsets (a warp reserves its slots with one atomicAdd).  The
