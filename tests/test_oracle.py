@@ -255,3 +255,38 @@ def test_port_composite_matches_reference_fragment_shader(rulesets, shape):
         want = P.composite(col, li, b)
         got = F.composite(P.mips(col), li, b)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_fullsize_batch_and_serve_fixtures_reproduce_on_the_port(ports):
+    """The batch4096 and serve entries of tests/golden/fullsize.json hold for the workloads
+    as workloads.py defines them today: their shape (4096 worlds, 149 sessions, 300
+    requests), and the port's digests of the eight smallest batch worlds after 100 frames
+    and of the two smallest serving sessions after all their requests."""
+    import json
+    from sandengine_gb300 import workloads as wl
+    from sandengine_gb300.simulation import grid_digest
+    with open(os.path.join(GOLDEN, "fullsize.json")) as f:
+        gold = json.load(f)
+    port = ports["twelve_materials"]
+    b = gold["batch4096"]
+    sizes = wl.batch_sizes(b["worlds"], 4)
+    assert len(sizes) == 4096 and all(len(cp["digests"]) == 4096 for cp in b["checkpoints"])
+    assert all(c["equal"] for c in b["reference_checks"])
+    spec = wl.twelve_fill_spec()
+    for i in sorted(range(len(sizes)), key=lambda i: sizes[i][0] * sizes[i][1])[:8]:
+        g = np.ascontiguousarray(wl.patch_fill(sizes[i][0], sizes[i][1], 1000 + i, *spec, patch=16), dtype=np.uint32)
+        port.run(g, b["frame0"], b["checkpoints"][0]["frames"], nthreads=8)
+        assert "%016x" % grid_digest(g) == b["checkpoints"][0]["digests"][i], f"batch world {i} {sizes[i]}"
+    s = gold["serve"]
+    sessions, reqs = wl.serve_requests(1.0, s["requests"])
+    assert len(sessions) == s["sessions"] == len(s["digests"]) and len(reqs) == 300
+    assert all(c["equal"] for c in s["reference_checks"])
+    for c in s["reference_checks"]:
+        sid = c["session"]
+        g = np.ascontiguousarray(wl.serve_session_grid(*sessions[sid], sid), dtype=np.uint32)
+        frame = 1
+        for s2, n, mods, _ in reqs:
+            if s2 == sid:
+                port.run(g, frame, n, mods or None, nthreads=8)
+                frame += n
+        assert "%016x" % grid_digest(g) == s["digests"][sid] and frame == s["frames"][sid], f"session {sid}"
