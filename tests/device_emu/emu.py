@@ -42,6 +42,20 @@ extern "C" uint32_t emu_lut_index_key(uint32_t i, uint32_t h0, uint32_t h1, uint
   return 0;
 #endif
 }
+// entries whose decoded cells and representative hashes do not index back to themselves
+extern "C" unsigned long long emu_lut_roundtrip_failures() {
+#ifdef SE_LUT
+  unsigned long long bad = 0;
+  for (uint32_t i = 0; i < SE_LUT_ENTRIES; ++i) {
+    uint32_t a, b, c, d, h0, h1, h2, h3;
+    se_gen::lut_decode(i, a, b, c, d, h0, h1, h2, h3);
+    if (se_gen::lut_index(a, b, c, d, h0, h1, h2, h3) != i) ++bad;
+  }
+  return bad;
+#else
+  return 0;
+#endif
+}
 extern "C" const uint32_t* emu_static() {
 #ifdef SE_LUT
   return reinterpret_cast<const uint32_t*>(reinterpret_cast<const uint8_t*>(g_lut) + SE_LUT_STATIC_OFF);

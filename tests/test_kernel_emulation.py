@@ -145,6 +145,18 @@ def test_narrow_table_keys_match_port(se, lut):
                 a = b
 
 
+@pytest.mark.parametrize("name", ["reference", "four_materials", "twelve_materials", "many_hash_classes"])
+def test_lut_decode_inverts_lut_index(se, rulesets, name):
+    """For every table entry, the cells and the representative hash values lut_decode gives
+    index back to that entry (the key layout and the class order agree between the table
+    build and the lookups)."""
+    import ctypes
+    E = Emu(se.parse_string(_text(rulesets, name)), lut=True)
+    assert E.has_lut
+    E.lib.emu_lut_roundtrip_failures.restype = ctypes.c_ulonglong
+    assert E.lib.emu_lut_roundtrip_failures() == 0
+
+
 @pytest.mark.parametrize("name", ["four_materials", "twelve_materials", "many_hash_classes"])
 def test_static_key_bitset(se, rulesets, name):
     """Bit `key` of se_build_static's bitset is set exactly when every table entry of that
